@@ -1,0 +1,155 @@
+/*
+ * voroffset_gpu.h -- C ABI of the GB300 (sm_103a) dexel morphology library.
+ *
+ * This is the drop-in boundary for Voroffset's 3D path: it replaces the
+ * reference's method layer (src/vor3d/Voronoi.h:13-44, class VoronoiMorpho and
+ * its implementations VoronoiMorphoVorPower "ours" and
+ * VoronoiMorphoBruteForce "brute_force") and the ray rasteriser
+ * (src/vor3d/Dexelize.h:25-28, create_dexels). Plain C types only: int32
+ * offsets and FP64 endpoint pairs, no C++ or torch types, no exceptions; every
+ * entry point returns a status code (VO_OK == 0) and records a message
+ * retrievable with vo_last_error().
+ *
+ * Data model (src/vor3d/CompressedVolume.h:28-29, CompressedVolumeBase.h:17-21):
+ *   a volume is an nx*ny grid of columns, column index c = x + nx*y; each
+ *   column is a sorted list of disjoint closed z-intervals [z1, z2] in dexel
+ *   units (absolute z / spacing). In CSR form: offs[nx*ny+1] (int32, counted
+ *   in segments, offs[0] == 0) and z[2*offs[nx*ny]] (FP64 pairs).
+ *   `origin` is the stored origin, already shifted by -padding*spacing the way
+ *   the CompressedVolume constructor leaves it (CompressedVolume.cpp:11-23).
+ *
+ * All device work of a context runs on the context's own CUDA stream, in
+ * order. A context must not be used from two host threads at once.
+ */
+#ifndef VOROFFSET_GPU_H
+#define VOROFFSET_GPU_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define VO_OK 0
+#define VO_EINVAL -1    /* bad argument */
+#define VO_ENOMEM -2    /* host or device allocation failed */
+#define VO_ECUDA -3     /* CUDA runtime error (message in vo_last_error) */
+#define VO_ERADIUS -4   /* radius a hair below a lattice distance (see DESIGN) */
+#define VO_ERANGE -5    /* result does not fit int32 CSR offsets */
+#define VO_ENODEV -6    /* no usable sm_103 device */
+#define VO_ETIMEOUT -7  /* a device-side bounded wait gave up */
+#define VO_EINTERNAL -8 /* internal consistency check failed */
+
+/* ---- operations (app/cli3d/offset3d.cpp:48-49, 116-136) ---- */
+#define VO_DILATION 0
+#define VO_EROSION 1
+#define VO_OPENING 2 /* erosion then dilation */
+#define VO_CLOSING 3 /* dilation then erosion */
+
+/* ---- methods ----
+ * VO_METHOD_SEPARABLE: the separable "ours" scheme (VoronoiVorPower.cpp:24-96),
+ *   FP64 end to end, count -> scan -> fill. Results match the reference's
+ *   FP64 CPU output (exact topology, endpoints within 1e-9).
+ * VO_METHOD_BRUTE: the lattice-disc brute force (VoronoiBruteForce.cpp:16-68),
+ *   the in-GPU cross-check.
+ * VO_METHOD_FAST: the separable scheme with FP32 envelope arithmetic guarded by
+ *   FP64 re-evaluation of near-tie merge/touch decisions (no reference
+ *   counterpart). */
+#define VO_METHOD_SEPARABLE 0
+#define VO_METHOD_BRUTE 1
+#define VO_METHOD_FAST 2
+
+typedef struct vo_ctx vo_ctx;
+typedef struct vo_volume vo_volume; /* a device-resident CSR volume */
+
+typedef struct {
+  int32_t nx, ny;
+  double origin[3];
+  double extent[3];
+  double spacing;
+  int32_t padding;
+} vo_grid;
+
+typedef struct {
+  double total_ms;  /* wall time of the call on the host */
+  double pass1_ms;  /* device time of the pass-1 kernels (time_1 of VoronoiVorPower.cpp:66) */
+  double pass2_ms;  /* device time of the pass-2 kernels (time_2 of VoronoiVorPower.cpp:95) */
+  int64_t in_segments;
+  int64_t mid_pieces; /* pass-1 intermediate size (summed over chained ops) */
+  int64_t out_segments;
+  int32_t kernel_launches; /* kernels this call launched */
+  int32_t overflow_columns; /* columns re-run through the large-capacity path */
+} vo_timings;
+
+/* Context (replaces std::make_unique<VoronoiMorphoVorPower>() at offset3d.cpp:104-112).
+ * device: CUDA ordinal; the device must be sm_103. */
+int vo_create(vo_ctx **ctx, int device);
+void vo_destroy(vo_ctx *ctx);
+/* Last error message of this context (never NULL; "" when none). */
+const char *vo_last_error(const vo_ctx *ctx);
+/* The context's cudaStream_t, as void*, so a host can order its own work or
+ * record events on it. */
+void *vo_stream(vo_ctx *ctx);
+/* Blocks until the context's stream is idle. */
+int vo_sync(vo_ctx *ctx);
+
+/* Volumes. Upload copies host CSR into a new device volume
+ * (the value semantics of VoronoiMorpho::dilation's by-value input, Voronoi.h:18). */
+int vo_volume_upload(vo_ctx *ctx, const vo_grid *grid, const int32_t *offs, const double *z,
+                     vo_volume **out);
+/* Grid and segment count of a volume (the size query before a download). */
+int vo_volume_info(vo_ctx *ctx, const vo_volume *v, vo_grid *grid, int64_t *nseg);
+/* Copies a volume to caller-allocated host buffers: offs[nx*ny+1], z[2*nseg]. */
+int vo_volume_download(vo_ctx *ctx, const vo_volume *v, int32_t *offs, double *z);
+/* Device pointers of a volume (offs: int32*, z: double*), valid until freed. */
+int vo_volume_device_ptrs(vo_ctx *ctx, const vo_volume *v, void **offs, void **z);
+void vo_volume_free(vo_ctx *ctx, vo_volume *v);
+
+/* Morphology (replaces VoronoiMorpho::dilation / erosion, Voronoi.h:18-29, and
+ * the opening/closing chaining of offset3d.cpp:124-133). radius in dexels.
+ * *out receives a new volume with the input's grid. timings may be NULL. */
+int vo_morph(vo_ctx *ctx, int op, int method, double radius, const vo_volume *in,
+             vo_volume **out, vo_timings *timings);
+
+/* Many independent volumes (uneven grids, radii and ops) in one call; no
+ * reference counterpart beyond calling vo_morph n times. */
+int vo_morph_batched(vo_ctx *ctx, int n, const int *ops, const double *radii, int method,
+                     const vo_volume *const *ins, vo_volume **outs, vo_timings *timings);
+
+/* Mesh -> dexels by vertical ray casting (replaces create_dexels + compute_sign,
+ * Dexelize.cpp:166-274). verts[3*nv] FP64, tris[3*nt] int32 (0-based).
+ * num_dexels > 0: spacing = longest bbox side / num_dexels; otherwise *spacing
+ * is used as given. *spacing returns the spacing used. */
+int vo_dexelize(vo_ctx *ctx, const double *verts, int nv, const int32_t *tris, int nt,
+                double *spacing, int padding, int num_dexels, vo_volume **out);
+
+/* Xor volume of two volumes on the same grid (Voronoi.cpp:91-111,
+ * calculateXor's return value), computed on the device. */
+int vo_xor_volume(vo_ctx *ctx, const vo_volume *a, const vo_volume *b, double *volume);
+
+/* ---- host utilities (no device work) ---- */
+
+/* Seeded synthetic volume: union of spheres and flat-capped cylinders
+ * evaluated at dexel centres, clipped to [0, zmax], merged per column. */
+typedef struct {
+  int32_t nx, ny;
+  double zmax;
+  int32_t n_spheres;
+  int32_t sphere_dist; /* 0: radius uniform in [s_rmin, s_rmax]; 1: lognormal(s_median, s_sigma) clipped */
+  double s_rmin, s_rmax, s_median, s_sigma;
+  int32_t n_cyl; /* endpoints uniform in the box, radius uniform in [c_rmin, c_rmax] */
+  double c_rmin, c_rmax;
+  uint64_t seed;
+} vo_synth_params;
+/* offs: caller array of nx*ny+1; *z is allocated (free with vo_host_free). */
+int vo_synth_volume(const vo_synth_params *p, int32_t *offs, double **z, int64_t *nseg);
+/* Watertight torus centred at (0.5,0.5,0.5), nu x nv quads split in triangles,
+ * vertices displaced along the normal by uniform noise in [-noise, noise]. */
+int vo_synth_torus(int nu, int nv, double major, double minor, double noise, uint64_t seed,
+                   double **verts, int *nverts, int32_t **tris, int *ntris);
+void vo_host_free(void *p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
