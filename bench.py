@@ -1,0 +1,344 @@
+"""Benchmark of the 3D dexel dilation path on GB300.
+
+One step = one dilation (radius 32 dexels) of the 2048 x 2048 synthetic volume
+"spheres_cyl2048" (16384 spheres, lognormal radii with median 12 clipped to
+[2, 80], plus 2000 random-axis cylinders of radius 1-4; seeded), the
+configuration the headline metric is quoted on. The input (~345 MB of FP64
+pairs) is larger than L2 (129 MB), so no flush is needed between steps.
+
+  value : Mcolumns/s with the input resident in HBM (device-timed, CUDA events
+          on the library's stream), whole job = all ranks.
+  e2e   : the same metric through the C ABI from pinned host buffers: upload,
+          dilation and download of the result inside the timed region.
+  cpu_baseline : the reference's own `ours` (oracle/_ref, multithreaded) or,
+          where the reference could not be built, the oracle restatement, timed
+          on a bounded slab of the same workload (rank 0, N=1).
+
+python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+Under torchrun each rank dilates its own replica (seed + rank): the path has
+no data exchange, so scaling is weak and replicas only.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "spheres_cyl2048"
+RADIUS = 32.0
+METRIC = "Mcolumns/s, 3D dilation 2048² r=32: plain vs batched+learned GPU, exact topology"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--method", default="separable", choices=["separable", "brute", "fast"])
+    ap.add_argument("--workload", default=WORKLOAD)
+    ap.add_argument("--radius", type=float, default=RADIUS)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU work of the baseline sample")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        sms, maxs, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sms.append(float(p[1]))
+                maxs.append(float(p[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sms:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sms)), "sm_max_mhz": float(max(maxs)), "reasons": sorted(reasons),
+                "samples": len(sms)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            p = json.load(fh)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_per_column(kernel: str, radius: float):
+    """DRAM bytes per output column of a kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic.json")
+    try:
+        with open(path) as fh:
+            d = json.load(fh)
+        e = d.get(f"{kernel}@r{int(radius)}")
+        return None if e is None else float(e["bytes_per_column"])
+    except Exception:
+        return None
+
+
+def cpu_sample(grid, offs, z, radius, target_s, step_rows=None):
+    """Times the CPU reference (or its restatement) on a slab of rows. Returns a dict."""
+    from oracle import oracle as O
+    kind = "reference" if O.ref_available() else "port"
+    cores = os.cpu_count() or 1
+    R = int(np.floor(radius))
+    nx, ny = grid.nx, grid.ny
+
+    def run(rows):
+        y0 = max(0, ny // 2 - rows // 2 - R)
+        y1 = min(ny, y0 + rows + 2 * R)
+        sub_offs = offs[y0 * nx:y1 * nx + 1] - offs[y0 * nx]
+        sub_z = z[2 * offs[y0 * nx]:2 * offs[y1 * nx]]
+        g = O.Grid(nx, y1 - y0, (0.0, 0.0, 0.0), (nx, y1 - y0, grid.extent[2]), 1.0, 0)
+        inner = nx * (y1 - y0)  # every slab column is computed by the same per-column work
+        t0 = time.perf_counter()
+        if kind == "reference":
+            O.ref_morph(g, sub_offs, sub_z, radius, "dilation", "ours", threads=cores)
+        else:
+            O.dilate_timed(g, sub_offs, sub_z, radius, threads=cores)
+        return time.perf_counter() - t0, inner, y1 - y0
+
+    if step_rows is None:
+        rows = 16
+        dt, inner, tot = run(rows)
+        while dt < target_s / 4 and rows < ny:
+            rows = min(ny, int(rows * max(2.0, 0.5 * target_s / max(dt, 1e-3))))
+            dt, inner, tot = run(rows)
+    else:
+        dt, inner, tot = run(step_rows)
+        rows = step_rows
+    val = inner / dt / 1e6
+    sample = (f"dilation r={radius:g} of a {nx} x {tot}-row slab cut from the middle of {WORKLOAD}, "
+              f"all {nx * tot} slab columns counted")
+    return {"value": val, "unit": "Mcolumns/s", "cores": cores, "kind": kind, "sample": sample,
+            "seconds": dt, "rows": rows}
+
+
+def reference_arm(args, rank, world):
+    if rank != 0:
+        return 0
+    import voroffset_gb300 as V
+    grid, offs, z = V.workload(args.workload, seed=1)
+    # calibrate a slab that takes a few seconds per step
+    cal = cpu_sample(grid, offs, z, args.radius, target_s=min(args.cpu_seconds, 8.0))
+    rows = cal["rows"]
+    vals = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_sample(grid, offs, z, args.radius, 0, step_rows=rows)
+        if i >= args.warmup:
+            vals.append(r)
+    secs = sum(r["seconds"] for r in vals)
+    cols = sum(r["value"] * r["seconds"] * 1e6 for r in vals)
+    value = cols / secs / 1e6
+    line = {"metric": METRIC, "value": value, "unit": "Mcolumns/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * secs / len(vals), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": f"{args.workload} dilation r={args.radius:g}", "grid": [grid.nx, grid.ny],
+                       "in_segments": int(offs[-1]), "parallelism": "host threads"},
+            "cpu_baseline": {"value": value, "unit": "Mcolumns/s", "cores": vals[0]["cores"],
+                             "kind": vals[0]["kind"], "sample": vals[0]["sample"]},
+            "e2e": {"value": value, "unit": "Mcolumns/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    if args.impl == "reference":
+        rc = reference_arm(args, rank, world)
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return rc
+
+    import torch
+    import voroffset_gb300 as V
+
+    torch.cuda.set_device(local)
+    grid, offs, z = V.workload(args.workload, seed=1 + rank)
+    ncols = grid.ncols
+    in_bytes = offs.nbytes + z.nbytes
+    ctx = V.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def maxreduce(x):
+        if world == 1:
+            return x
+        import torch.distributed as dist
+        t = torch.tensor([x], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---------------- device-resident arm (value)
+    vin = ctx.upload(grid, offs, z)
+    ctx.sync()
+    for _ in range(args.warmup):
+        out, t = ctx.morph(vin, "dilation", args.radius, args.method)
+        out.free()
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    launches = 0
+    kms = np.zeros(4)
+    tims = []
+    out_segs = 0
+    mid = 0
+    for _ in range(args.steps):
+        out, t = ctx.morph(vin, "dilation", args.radius, args.method)
+        launches += t["kernel_launches"]
+        kms += np.array(t["kernel_ms"])
+        tims.append(t)
+        out_segs = out.nseg
+        mid = t["mid_pieces"]
+        out.free()
+    ev1.record(stream)
+    barrier()
+    clk = clocks.stop()
+    dev_ms = ev0.elapsed_time(ev1)
+    dev_ms = maxreduce(dev_ms)
+    value = world * ncols * args.steps / (dev_ms / 1e3) / 1e6
+
+    # ---------------- end-to-end arm (pinned host buffers through the C ABI)
+    pin_offs = torch.empty(offs.size, dtype=torch.int32, pin_memory=True).numpy()
+    pin_z = torch.empty(max(z.size, 2), dtype=torch.float64, pin_memory=True).numpy()
+    pin_offs[:] = offs
+    pin_z[:z.size] = z
+    out_offs = torch.empty(ncols + 1, dtype=torch.int32, pin_memory=True).numpy()
+    out_z = torch.empty(max(2 * out_segs, 2), dtype=torch.float64, pin_memory=True).numpy()
+    for _ in range(max(1, args.warmup)):
+        v = ctx.upload(grid, pin_offs, pin_z[:z.size])
+        o, _ = ctx.morph(v, "dilation", args.radius, args.method)
+        ctx.download_into(o, out_offs, out_z)
+        o.free()
+        v.free()
+    barrier()
+    t0 = time.perf_counter()
+    d2h = 0
+    for _ in range(args.steps):
+        v = ctx.upload(grid, pin_offs, pin_z[:z.size])
+        o, _ = ctx.morph(v, "dilation", args.radius, args.method)
+        n_o, n_z = ctx.download_into(o, out_offs, out_z)
+        d2h = 4 * n_o + 8 * n_z
+        o.free()
+        v.free()
+    barrier()
+    e2e_s = maxreduce(time.perf_counter() - t0)
+    e2e = world * ncols * args.steps / e2e_s / 1e6
+
+    # ---------------- roofline of the dominant kernel
+    names = ["pass1_count", "pass1_fill", "pass2_count", "pass2_fill"]
+    per_launch = kms / args.steps
+    dom = int(np.argmax(per_launch))
+    alg_bytes = 4 * (ncols + 1) + 16 * int(offs[-1]) + 4 * (ncols + 1) + 16 * int(out_segs)
+    peak, peak_kind = peaks()
+    achieved = alg_bytes / (per_launch[dom] / 1e3) / 1e9 if per_launch[dom] > 0 else 0.0
+    tpc = traffic_per_column(names[dom], args.radius)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": None if tpc is None else tpc * ncols,
+                "kernel": names[dom], "kernel_ms": per_launch[dom], "peak_source": peak_kind,
+                "algorithmic_bytes": alg_bytes,
+                "op_achieved": alg_bytes / (dev_ms / args.steps / 1e3) / 1e9}
+
+    line = {"metric": METRIC, "value": value, "unit": "Mcolumns/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.method != "fast" else "f32+f64",
+            "data": "synthetic",
+            "config": {"workload": f"{args.workload} dilation r={args.radius:g}", "grid": [grid.nx, grid.ny],
+                       "method": args.method, "in_segments": int(offs[-1]), "out_segments": int(out_segs),
+                       "mid_pieces": int(mid), "l2": "inputs larger than L2 (no flush)",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "e2e": {"value": e2e, "unit": "Mcolumns/s", "h2d_bytes_per_step": int(in_bytes),
+                    "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": int(launches),
+            "kernel_ms_per_step": {n: float(x) for n, x in zip(names, per_launch)},
+            "roofline": roofline, "clocks": clk,
+            "gsegments_per_s": world * (int(offs[-1]) + int(out_segs)) * args.steps / (dev_ms / 1e3) / 1e9}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        try:
+            line["cpu_baseline"] = {k: v for k, v in cpu_sample(grid, offs, z, args.radius,
+                                                               args.cpu_seconds).items() if k != "rows"}
+        except Exception as exc:  # the baseline is reported, never required
+            line["cpu_baseline"] = {"value": None, "error": str(exc)}
+    vin.free()
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -79,6 +79,10 @@ typedef struct {
   int64_t out_segments;
   int32_t kernel_launches; /* kernels this call launched */
   int32_t overflow_columns; /* columns re-run through the large-capacity path */
+  /* device time (CUDA events on the context stream) of the pass-1 count,
+   * pass-1 fill, pass-2 count and pass-2 fill kernels, summed over the call
+   * (brute force: [2] count, [3] fill) */
+  double kernel_ms[4];
 } vo_timings;
 
 /* Context (replaces std::make_unique<VoronoiMorphoVorPower>() at offset3d.cpp:104-112).

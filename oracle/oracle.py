@@ -94,6 +94,7 @@ def lib():
         L.vo_or_xor_volume.restype = C.c_double
         L.vo_or_get_volume.argtypes = [G, V]
         L.vo_or_get_volume.restype = C.c_double
+        L.vo_or_dilate_columns.argtypes = [G, V, C.c_double, C.POINTER(C.c_int32), C.c_int, C.c_int, V]
         L.vo_or_pass1_pieces.argtypes = [G, V, C.c_double, C.c_int]
         L.vo_or_pass1_pieces.restype = C.c_int64
         L.vo_or_dexelize.argtypes = [C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_int32), C.c_int,
@@ -175,6 +176,19 @@ def dilate_timed(grid: Grid, offs, z, radius: float, threads: int = 0):
     _rc(rc, "vo_or_dilate")
     o, zz = _csr_take(cout, grid.nx * grid.ny)
     return o, zz, t1.value, t2.value
+
+
+def dilate_columns(grid: Grid, offs, z, radius: float, cols, threads: int = 0):
+    """Separable dilation of the selected output columns only: returns (offs[len(cols)+1], z)."""
+    L = lib()
+    cols = np.ascontiguousarray(cols, dtype=np.int32)
+    cin, keep = _csr_in(offs, z)
+    cout = _Csr()
+    rc = L.vo_or_dilate_columns(C.byref(grid.to_c()), C.byref(cin), float(radius),
+                                cols.ctypes.data_as(C.POINTER(C.c_int32)), int(cols.size),
+                                threads or os.cpu_count(), C.byref(cout))
+    _rc(rc, "vo_or_dilate_columns")
+    return _csr_take(cout, int(cols.size))
 
 
 def pass1_pieces(grid: Grid, offs, z, radius: float, threads: int = 0) -> int:

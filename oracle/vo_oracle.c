@@ -326,7 +326,7 @@ static int pass2_column(int nx, const pieces_csr *pc, const tables *t, int x, in
           continue;
         }
         double lo = p1 - h, hi = p2 + h;
-        if (open && lo <= ghi) {
+        if (open && lo <= ghi && hi >= glo) {
           if (lo < glo) glo = lo;
           if (hi > ghi) ghi = hi;
         } else {
@@ -525,6 +525,67 @@ int vo_or_dilate(const vo_or_grid *g, const vo_or_csr *in, double radius, int nt
   free(poffs);
   free(pv);
   free(pd);
+  tables_free(&t);
+  return rc;
+}
+
+/* Separable dilation restricted to selected output columns: for each one, the
+ * pass-1 pieces of the 2*Dx[0]+1 source columns of its row are built on the
+ * fly, then pass 2 runs on that one-row window. Same arithmetic as
+ * vo_or_dilate; used for exact checks of full-size GPU results on a sample. */
+typedef struct {
+  int nx, ny;
+  const vo_or_csr *in;
+  const tables *t;
+  const int32_t *cols;
+} sel_ctx;
+
+static int sel_fn(void *vctx, int i, scratch *s, pvec *outp, ivec *outi) {
+  (void)outp;
+  sel_ctx *x = (sel_ctx *)vctx;
+  const int c = x->cols[i];
+  const int cx = c % x->nx, cy = c / x->nx, W = x->t->W;
+  const int x0 = cx - (W - 1) < 0 ? 0 : cx - (W - 1);
+  const int x1 = cx + (W - 1) > x->nx - 1 ? x->nx - 1 : cx + (W - 1);
+  const int nw = x1 - x0 + 1;
+  int32_t *woffs = (int32_t *)malloc(sizeof(int32_t) * (nw + 1));
+  pvec all = {0};
+  if (!woffs) return -1;
+  woffs[0] = 0;
+  for (int k = 0; k < nw; ++k) {
+    if (pass1_column(x->nx, x->ny, x->in, x->t, x0 + k, cy, s)) {
+      free(woffs);
+      return -1;
+    }
+    for (int j = 0; j < s->P.n; ++j)
+      if (pvec_push(&all, s->P.v[2 * j], s->P.v[2 * j + 1], s->P.d[j])) {
+        free(woffs);
+        return -1;
+      }
+    woffs[k + 1] = all.n;
+  }
+  pieces_csr pc = {woffs, all.v, all.d};
+  int rc = pass2_column(nw, &pc, x->t, cx - x0, 0, &s->A);
+  free(woffs);
+  free(all.v);
+  free(all.d);
+  if (rc) return -1;
+  for (int k = 0; k < s->A.n; ++k)
+    if (ivec_push(outi, s->A.v[2 * k], s->A.v[2 * k + 1])) return -1;
+  return 0;
+}
+
+int vo_or_dilate_columns(const vo_or_grid *g, const vo_or_csr *in, double radius, const int32_t *cols,
+                         int ncols_sel, int nthreads, vo_or_csr *out) {
+  if (!g || !in || !cols || !out || ncols_sel < 0) return VO_OR_EINVAL;
+  for (int i = 0; i < ncols_sel; ++i)
+    if (cols[i] < 0 || cols[i] >= g->nx * g->ny) return VO_OR_EINVAL;
+  tables t;
+  int rc = tables_build(radius, kmax_of(g), &t);
+  if (rc) return rc;
+  sel_ctx ctx = {g->nx, g->ny, in, &t, cols};
+  pdriver D = {ncols_sel, nthreads, sel_fn, &ctx, 0, NULL, NULL, NULL, 0};
+  rc = pdrive(&D, &out->offs, &out->z, NULL);
   tables_free(&t);
   return rc;
 }

@@ -40,6 +40,9 @@ typedef struct {
 /* Separable ("ours") dilation semantics, restated as an exact union. */
 int vo_or_dilate(const vo_or_grid *g, const vo_or_csr *in, double radius, int nthreads,
                  vo_or_csr *out, double *t1_ms, double *t2_ms);
+/* Separable dilation of selected output columns only (out CSR has ncols_sel+1 offsets). */
+int vo_or_dilate_columns(const vo_or_grid *g, const vo_or_csr *in, double radius, const int32_t *cols,
+                         int ncols_sel, int nthreads, vo_or_csr *out);
 /* Brute-force lattice-disc dilation (VoronoiBruteForce.cpp:16-100). */
 int vo_or_dilate_brute(const vo_or_grid *g, const vo_or_csr *in, double radius, int nthreads,
                        vo_or_csr *out);

@@ -1,0 +1,374 @@
+// C ABI of libvoroffset_gpu.so (include/voroffset_gpu.h): contexts, device
+// volumes, radius tables and operation chaining. The kernels live in
+// vo_morph.cu (morphology), vo_dexel.cu (ray rasterisation) and vo_reduce.cu
+// (xor volume).
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "vo_internal.cuh"
+
+namespace vo {
+
+int set_error(vo_ctx *ctx, int code, const std::string &msg) {
+  if (ctx) ctx->err = msg;
+  return code;
+}
+
+int cuda_error(vo_ctx *ctx, cudaError_t e, const char *where) {
+  std::string m = std::string(where) + ": " + cudaGetErrorString(e);
+  cudaGetLastError();  // clear a sticky-free error so the context stays usable
+  return set_error(ctx, VO_ECUDA, m);
+}
+
+void dfree(vo_ctx *ctx, void *p) {
+  if (p) cudaFreeAsync(p, ctx->stream);
+}
+
+// Host tables with the reference's expressions (compiled with
+// -ffp-contract=off so a*b - c*d is never fused):
+//   pass-1 radius (Voronoi2D.cpp:704-712): r = d==0 ? R : sqrt(R*R - dd*dd), dd = min(d, R)
+//   pass-2 half width (SeparatePower2D.cpp:314): sqrt(r*r - dx*dx)
+//   brute force (VoronoiBruteForce.cpp:41-52): sqrt(R*R - dx^2 - dy^2) inside the disc
+//   expiry (Voronoi2D.cpp:619, SeparatePower2D.cpp:266): alive while floor(x_s + r) + 1 > i
+int build_tables(double R, int kmax, Tables &t) {
+  t = Tables();
+  if (!(R >= 0.0) || R > 255.0) return VO_EINVAL;
+  t.R = R;
+  t.Dy = (int)std::floor(R);
+  for (int k = 0; k < kmax; ++k)
+    if ((int)std::floor((double)k + R) != k + t.Dy) return VO_ERADIUS;
+  const int Dy = t.Dy;
+  t.r1.resize(Dy + 1);
+  t.Dx.resize(Dy + 1);
+  for (int d = 0; d <= Dy; ++d) {
+    if (d == 0) {
+      t.r1[d] = R;
+    } else {
+      const double dd = (double)d < R ? (double)d : R;
+      t.r1[d] = std::sqrt(R * R - dd * dd);
+    }
+    t.Dx[d] = (int)std::floor(t.r1[d]);
+    for (int k = 0; k < kmax; ++k)
+      if ((int)std::floor((double)k + t.r1[d]) != k + t.Dx[d]) return VO_ERADIUS;
+  }
+  t.W = t.Dx[0] + 1;
+  t.H.assign((size_t)(Dy + 1) * t.W, NAN);
+  t.Hf.assign(t.H.size(), NAN);
+  for (int d = 0; d <= Dy; ++d)
+    for (int dx = 0; dx <= t.Dx[d]; ++dx) {
+      const double r = t.r1[d], x = (double)dx;
+      t.H[(size_t)d * t.W + dx] = std::sqrt(r * r - x * x);
+      t.Hf[(size_t)d * t.W + dx] = (float)t.H[(size_t)d * t.W + dx];
+    }
+  t.HB.assign((size_t)(Dy + 1) * (Dy + 1), NAN);
+  for (int dy = 0; dy <= Dy; ++dy)
+    for (int dx = 0; dx <= Dy; ++dx) {
+      const double fx = (double)dx * dx, fy = (double)dy * dy;
+      if (fx + fy <= R * R) t.HB[(size_t)dy * (Dy + 1) + dx] = std::sqrt(R * R - fx - fy);
+    }
+  return VO_OK;
+}
+
+int get_tables(vo_ctx *ctx, double R, int kmax, const DeviceTables **out) {
+  for (DeviceTables *d : ctx->tables)
+    if (d->R == R && d->kmax >= kmax) {
+      *out = d;
+      return VO_OK;
+    }
+  Tables h;
+  int rc = build_tables(R, kmax, h);
+  if (rc == VO_EINVAL) return set_error(ctx, rc, "radius must be in [0, 255] dexels");
+  if (rc == VO_ERADIUS) {
+    char b[160];
+    std::snprintf(b, sizeof b,
+                  "radius %.17g lies within rounding of a lattice distance; its reach would "
+                  "depend on the column position",
+                  R);
+    return set_error(ctx, rc, b);
+  }
+  DeviceTables *d = new (std::nothrow) DeviceTables();
+  if (!d) return set_error(ctx, VO_ENOMEM, "host allocation");
+  d->R = R;
+  d->kmax = kmax;
+  d->host = h;
+  cudaError_t e = cudaMalloc(&d->H, sizeof(double) * h.H.size());
+  if (e == cudaSuccess) e = cudaMalloc(&d->Hf, sizeof(float) * h.Hf.size());
+  if (e == cudaSuccess) e = cudaMalloc(&d->Dx, sizeof(int) * h.Dx.size());
+  if (e == cudaSuccess) e = cudaMalloc(&d->HB, sizeof(double) * h.HB.size());
+  if (e == cudaSuccess)
+    e = cudaMemcpy(d->H, h.H.data(), sizeof(double) * h.H.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(d->Hf, h.Hf.data(), sizeof(float) * h.Hf.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(d->Dx, h.Dx.data(), sizeof(int) * h.Dx.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(d->HB, h.HB.data(), sizeof(double) * h.HB.size(), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(d->H);
+    cudaFree(d->Hf);
+    cudaFree(d->Dx);
+    cudaFree(d->HB);
+    delete d;
+    return cuda_error(ctx, e, "table upload");
+  }
+  if (ctx->tables.size() >= 16) {
+    DeviceTables *old = ctx->tables.front();
+    cudaFree(old->H);
+    cudaFree(old->Hf);
+    cudaFree(old->Dx);
+    cudaFree(old->HB);
+    delete old;
+    ctx->tables.erase(ctx->tables.begin());
+  }
+  ctx->tables.push_back(d);
+  *out = d;
+  return VO_OK;
+}
+
+int volume_alloc(vo_ctx *ctx, const vo_grid &g, int64_t nseg, vo_volume **out) {
+  vo_volume *v = new (std::nothrow) vo_volume();
+  if (!v) return set_error(ctx, VO_ENOMEM, "host allocation");
+  v->grid = g;
+  v->nseg = nseg;
+  const size_t ncols = (size_t)g.nx * g.ny;
+  int rc = dalloc(ctx, &v->offs, ncols + 1);
+  if (!rc && nseg > 0) rc = dalloc(ctx, &v->z, (size_t)nseg);
+  if (rc) {
+    dfree(ctx, v->offs);
+    delete v;
+    return rc;
+  }
+  *out = v;
+  return VO_OK;
+}
+
+}  // namespace vo
+
+using namespace vo;
+
+namespace {
+
+bool grid_ok(const vo_grid *g) {
+  return g && g->nx > 0 && g->ny > 0 && (int64_t)g->nx * g->ny < (1ll << 31) - 1 &&
+         g->spacing > 0 && std::isfinite(g->spacing);
+}
+
+}  // namespace
+
+extern "C" {
+
+int vo_create(vo_ctx **out, int device) {
+  if (!out) return VO_EINVAL;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) {
+    cudaGetLastError();
+    return VO_ENODEV;
+  }
+  if (device < 0 || device >= n) return VO_EINVAL;
+  cudaDeviceProp p;
+  if (cudaGetDeviceProperties(&p, device) != cudaSuccess) return VO_ENODEV;
+  if (!(p.major == 10 && p.minor == 3)) return VO_ENODEV;  // built for sm_103a only
+  vo_ctx *ctx = new (std::nothrow) vo_ctx();
+  if (!ctx) return VO_ENOMEM;
+  ctx->device = device;
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete ctx;
+    return VO_ECUDA;
+  }
+  for (auto &e : ctx->ev) cudaEventCreate(&e);
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t thr = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  if (cudaMalloc(&ctx->d_flags, 16 * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&ctx->d_total, 4 * sizeof(long long)) != cudaSuccess ||
+      cudaMallocHost(&ctx->h_total, 4 * sizeof(long long)) != cudaSuccess) {
+    vo_destroy(ctx);
+    return VO_ENOMEM;
+  }
+  cudaMemset(ctx->d_flags, 0, 16 * sizeof(int));
+  *out = ctx;
+  return VO_OK;
+}
+
+void vo_destroy(vo_ctx *ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  for (DeviceTables *d : ctx->tables) {
+    cudaFree(d->H);
+    cudaFree(d->Hf);
+    cudaFree(d->Dx);
+    cudaFree(d->HB);
+    delete d;
+  }
+  for (auto &e : ctx->ev)
+    if (e) cudaEventDestroy(e);
+  cudaFree(ctx->d_flags);
+  cudaFree(ctx->d_total);
+  if (ctx->h_total) cudaFreeHost(ctx->h_total);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+const char *vo_last_error(const vo_ctx *ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+void *vo_stream(vo_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+int vo_sync(vo_ctx *ctx) {
+  if (!ctx) return VO_EINVAL;
+  VO_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  return VO_OK;
+}
+
+int vo_volume_upload(vo_ctx *ctx, const vo_grid *grid, const int32_t *offs, const double *z,
+                     vo_volume **out) {
+  if (!ctx || !out || !offs || !grid_ok(grid)) return set_error(ctx, VO_EINVAL, "upload: bad grid");
+  *out = nullptr;
+  const int64_t ncols = (int64_t)grid->nx * grid->ny;
+  if (offs[0] != 0) return set_error(ctx, VO_EINVAL, "upload: offs[0] must be 0");
+  for (int64_t c = 0; c < ncols; ++c)
+    if (offs[c + 1] < offs[c]) return set_error(ctx, VO_EINVAL, "upload: offsets must not decrease");
+  const int64_t nseg = offs[ncols];
+  if (nseg > 0 && !z) return set_error(ctx, VO_EINVAL, "upload: z is NULL");
+  cudaSetDevice(ctx->device);
+  vo_volume *v = nullptr;
+  int rc = volume_alloc(ctx, *grid, nseg, &v);
+  if (rc) return rc;
+  cudaError_t e = cudaMemcpyAsync(v->offs, offs, sizeof(int32_t) * (ncols + 1),
+                                  cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess && nseg > 0)
+    e = cudaMemcpyAsync(v->z, z, sizeof(double) * 2 * nseg, cudaMemcpyHostToDevice, ctx->stream);
+  if (e != cudaSuccess) {
+    vo_volume_free(ctx, v);
+    return cuda_error(ctx, e, "upload");
+  }
+  *out = v;
+  return VO_OK;
+}
+
+int vo_volume_info(vo_ctx *ctx, const vo_volume *v, vo_grid *grid, int64_t *nseg) {
+  if (!ctx || !v) return VO_EINVAL;
+  if (grid) *grid = v->grid;
+  if (nseg) *nseg = v->nseg;
+  return VO_OK;
+}
+
+int vo_volume_download(vo_ctx *ctx, const vo_volume *v, int32_t *offs, double *z) {
+  if (!ctx || !v || !offs || (v->nseg > 0 && !z)) return set_error(ctx, VO_EINVAL, "download: NULL buffer");
+  cudaSetDevice(ctx->device);
+  const int64_t ncols = (int64_t)v->grid.nx * v->grid.ny;
+  VO_CK(ctx, cudaMemcpyAsync(offs, v->offs, sizeof(int32_t) * (ncols + 1), cudaMemcpyDeviceToHost,
+                             ctx->stream));
+  if (v->nseg > 0)
+    VO_CK(ctx, cudaMemcpyAsync(z, v->z, sizeof(double) * 2 * v->nseg, cudaMemcpyDeviceToHost,
+                               ctx->stream));
+  VO_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  return VO_OK;
+}
+
+int vo_volume_device_ptrs(vo_ctx *ctx, const vo_volume *v, void **offs, void **z) {
+  if (!ctx || !v) return VO_EINVAL;
+  if (offs) *offs = v->offs;
+  if (z) *z = v->z;
+  return VO_OK;
+}
+
+void vo_volume_free(vo_ctx *ctx, vo_volume *v) {
+  if (!ctx || !v) return;
+  if (v->owns) {
+    dfree(ctx, v->offs);
+    dfree(ctx, v->z);
+  }
+  delete v;
+}
+
+int vo_morph(vo_ctx *ctx, int op, int method, double radius, const vo_volume *in, vo_volume **out,
+             vo_timings *tm) {
+  if (!ctx) return VO_EINVAL;
+  if (!in || !out) return set_error(ctx, VO_EINVAL, "morph: NULL volume");
+  if (op < VO_DILATION || op > VO_CLOSING) return set_error(ctx, VO_EINVAL, "morph: unknown op");
+  if (method != VO_METHOD_SEPARABLE && method != VO_METHOD_BRUTE)
+    return set_error(ctx, VO_EINVAL, "morph: unknown method");
+  if (!(radius >= 0) || radius > 255) return set_error(ctx, VO_EINVAL, "morph: radius must be in [0, 255]");
+  cudaSetDevice(ctx->device);
+  *out = nullptr;
+  ctx->err.clear();
+  ctx->launches = 0;
+  ctx->ovf_cols = 0;
+  vo_timings local;
+  std::memset(&local, 0, sizeof local);
+  vo_timings *t = tm ? tm : &local;
+  std::memset(t, 0, sizeof *t);
+  const auto t0 = std::chrono::steady_clock::now();
+  vo_volume *tmp = nullptr;
+  int rc;
+  switch (op) {
+    case VO_DILATION:
+      rc = dilate(ctx, method, radius, in, out, t);
+      break;
+    case VO_EROSION:
+      rc = erode(ctx, method, radius, in, out, t);
+      break;
+    case VO_OPENING:
+      rc = erode(ctx, method, radius, in, &tmp, t);
+      if (!rc) rc = dilate(ctx, method, radius, tmp, out, t);
+      break;
+    default:  // VO_CLOSING
+      rc = dilate(ctx, method, radius, in, &tmp, t);
+      if (!rc) rc = erode(ctx, method, radius, tmp, out, t);
+      break;
+  }
+  if (tmp) vo_volume_free(ctx, tmp);
+  if (!rc) {
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) rc = cuda_error(ctx, e, "morph");
+  }
+  t->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  t->in_segments = in->nseg;
+  t->out_segments = (!rc && *out) ? (*out)->nseg : 0;
+  t->kernel_launches = ctx->launches;
+  t->overflow_columns = ctx->ovf_cols;
+  if (rc && *out) {
+    vo_volume_free(ctx, *out);
+    *out = nullptr;
+  }
+  return rc;
+}
+
+int vo_morph_batched(vo_ctx *ctx, int n, const int *ops, const double *radii, int method,
+                     const vo_volume *const *ins, vo_volume **outs, vo_timings *tm) {
+  if (!ctx || n < 0 || (n > 0 && (!ops || !radii || !ins || !outs))) return VO_EINVAL;
+  vo_timings acc;
+  std::memset(&acc, 0, sizeof acc);
+  for (int i = 0; i < n; ++i) outs[i] = nullptr;
+  for (int i = 0; i < n; ++i) {
+    vo_timings t;
+    int rc = vo_morph(ctx, ops[i], method, radii[i], ins[i], &outs[i], &t);
+    if (rc) {
+      for (int j = 0; j < i; ++j) {
+        vo_volume_free(ctx, outs[j]);
+        outs[j] = nullptr;
+      }
+      return rc;
+    }
+    acc.total_ms += t.total_ms;
+    acc.pass1_ms += t.pass1_ms;
+    acc.pass2_ms += t.pass2_ms;
+    acc.in_segments += t.in_segments;
+    acc.mid_pieces += t.mid_pieces;
+    acc.out_segments += t.out_segments;
+    acc.kernel_launches += t.kernel_launches;
+    acc.overflow_columns += t.overflow_columns;
+  }
+  if (tm) *tm = acc;
+  return VO_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,122 @@
+// Internal declarations shared by the CUDA translation units of
+// libvoroffset_gpu.so. Not part of the public ABI (include/voroffset_gpu.h).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "voroffset_gpu.h"
+
+namespace vo {
+
+// Per-thread capacities of the in-register/local-memory working lists. A
+// column that needs more is flagged and re-run by the large-capacity variant
+// of the same kernel, whose lists live in global scratch.
+constexpr int kCapSmall = 32;    // pass-1 touching-merged piece list / pass-2 union
+constexpr int kCapLarge = 2048;  // overflow re-run capacity per column
+
+// Radius tables, computed on the host with the reference's own FP64
+// expressions (so device results match bit for bit) and uploaded once per
+// (radius, grid extent).
+struct Tables {
+  double R = 0;
+  int Dy = 0;                 // max pass-1 lattice distance (floor(R))
+  int W = 0;                  // Dx[0] + 1 (row stride of H)
+  std::vector<double> r1;     // [Dy+1] pass-1 radius per label
+  std::vector<int> Dx;        // [Dy+1] max |dx| per label
+  std::vector<double> H;      // [(Dy+1)*W] sqrt(r1*r1 - dx*dx), NaN beyond Dx
+  std::vector<float> Hf;      // FP32 rounding of H
+  std::vector<double> HB;     // [(Dy+1)^2] brute force sqrt(R*R - dx^2 - dy^2), NaN outside
+};
+
+// Device view of the tables (kernel argument by value).
+struct DevTables {
+  int Dy, W;
+  const double *H;
+  const float *Hf;
+  const int *Dx;
+  const double *HB;
+};
+
+// Builds tables for radius R serving sweep indices 0..kmax-1; returns VO_OK,
+// VO_EINVAL or VO_ERADIUS.
+int build_tables(double R, int kmax, Tables &t);
+
+struct DeviceTables {
+  double R = -1;
+  int kmax = 0;
+  double *H = nullptr;
+  float *Hf = nullptr;
+  int *Dx = nullptr;
+  double *HB = nullptr;
+  Tables host;
+  DevTables view() const { return DevTables{host.Dy, host.W, H, Hf, Dx, HB}; }
+};
+
+}  // namespace vo
+
+struct vo_volume {
+  vo_grid grid;
+  int64_t nseg = 0;      // host-known segment count
+  int32_t *offs = nullptr;  // device [nx*ny+1]
+  double2 *z = nullptr;     // device [nseg]
+  bool owns = true;
+};
+
+struct vo_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  std::vector<vo::DeviceTables *> tables;  // small cache keyed by (R, kmax)
+  cudaEvent_t ev[8] = {};
+  int launches = 0;  // kernel launches of the current call
+  int ovf_cols = 0;
+  // persistent small device scratch
+  int *d_flags = nullptr;  // [0]: overflow count, [1..]: misc status
+  long long *d_total = nullptr;
+  long long *h_total = nullptr;  // pinned
+};
+
+namespace vo {
+
+// Error helpers: set ctx->err and return a status.
+int set_error(vo_ctx *ctx, int code, const std::string &msg);
+int cuda_error(vo_ctx *ctx, cudaError_t e, const char *where);
+
+#define VO_CK(ctx, call)                                 \
+  do {                                                   \
+    cudaError_t e_ = (call);                             \
+    if (e_ != cudaSuccess) return vo::cuda_error((ctx), e_, #call); \
+  } while (0)
+
+// Stream-ordered allocation helpers on ctx->stream.
+template <typename T>
+int dalloc(vo_ctx *ctx, T **p, size_t n) {
+  *p = nullptr;
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMallocAsync((void **)p, n * sizeof(T), ctx->stream);
+  if (e != cudaSuccess) return cuda_error(ctx, e, "cudaMallocAsync");
+  return VO_OK;
+}
+void dfree(vo_ctx *ctx, void *p);
+
+// Tables for radius R, cached in the context.
+int get_tables(vo_ctx *ctx, double R, int kmax, const DeviceTables **out);
+
+// Exclusive scan of int32 counts into int32 offsets (n+1 entries); the total
+// is returned through ctx->h_total (synchronising read). Returns VO_ERANGE if
+// the total exceeds INT32_MAX.
+int scan_counts(vo_ctx *ctx, const int32_t *counts, int32_t *offs, int n, long long *total);
+
+// Morphology drivers (vo_morph.cu).
+int dilate(vo_ctx *ctx, int method, double R, const vo_volume *in, vo_volume **out,
+           vo_timings *tm);
+int erode(vo_ctx *ctx, int method, double R, const vo_volume *in, vo_volume **out,
+          vo_timings *tm);
+
+// Volume allocation (vo_api.cu).
+int volume_alloc(vo_ctx *ctx, const vo_grid &g, int64_t nseg, vo_volume **out);
+
+}  // namespace vo
