@@ -44,7 +44,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--method", default="separable", choices=["separable", "brute", "fast"])
+    ap.add_argument("--method", default="fast", choices=["separable", "brute", "fast"])
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--radius", type=float, default=RADIUS)
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -495,6 +495,63 @@ static int pass2_fn(void *vctx, int c, scratch *s, pvec *outp, ivec *outi) {
 
 static int kmax_of(const vo_or_grid *g) { return (g->nx > g->ny ? g->nx : g->ny) + 2; }
 
+static int cmp_pair(const void *a, const void *b) {
+  const double *x = (const double *)a, *y = (const double *)b;
+  if (x[0] != y[0]) return x[0] < y[0] ? -1 : 1;
+  return x[1] < y[1] ? -1 : (x[1] > y[1] ? 1 : 0);
+}
+
+/* Inverted pairs [a, b], a > b, appear when erosion complements a column whose
+ * values left [zmin, zmax] (negate_ray, MorphologyOperators.cpp:230-259). The
+ * reference's pass 2 then only sees their two endpoint circles
+ * (SeparatePower2D.cpp:215-226 inserts both endpoints as points), so they are
+ * rewritten as the points [b, b] and [a, a]; columns that contain one are
+ * re-sorted and merged as closed intervals. Columns without inverted pairs
+ * are copied unchanged. Returns 1 if anything was rewritten (and fills out). */
+static int normalize_inverted(int ncols, const vo_or_csr *in, vo_or_csr *out) {
+  int64_t nseg = in->offs[ncols], ninv = 0;
+  for (int64_t k = 0; k < nseg; ++k)
+    if (in->z[2 * k] > in->z[2 * k + 1]) ++ninv;
+  if (!ninv) return 0;
+  out->offs = (int32_t *)malloc(sizeof(int32_t) * ((size_t)ncols + 1));
+  out->z = (double *)malloc(sizeof(double) * 2 * (size_t)(nseg + ninv + 1));
+  double *tmp = (double *)malloc(sizeof(double) * 2 * (size_t)(nseg + ninv + 1));
+  if (!out->offs || !out->z || !tmp) {
+    free(out->offs);
+    free(out->z);
+    free(tmp);
+    return -1;
+  }
+  int64_t w = 0;
+  out->offs[0] = 0;
+  for (int c = 0; c < ncols; ++c) {
+    int n = 0;
+    for (int k = in->offs[c]; k < in->offs[c + 1]; ++k) {
+      double a = in->z[2 * k], b = in->z[2 * k + 1];
+      if (a > b) {
+        tmp[2 * n] = b, tmp[2 * n + 1] = b, ++n;
+        tmp[2 * n] = a, tmp[2 * n + 1] = a, ++n;
+      } else {
+        tmp[2 * n] = a, tmp[2 * n + 1] = b, ++n;
+      }
+    }
+    qsort(tmp, n, 2 * sizeof(double), cmp_pair);
+    int64_t c0 = w;
+    for (int k = 0; k < n; ++k) {
+      if (w > c0 && !(out->z[2 * w - 1] < tmp[2 * k])) {
+        if (tmp[2 * k + 1] > out->z[2 * w - 1]) out->z[2 * w - 1] = tmp[2 * k + 1];
+      } else {
+        out->z[2 * w] = tmp[2 * k];
+        out->z[2 * w + 1] = tmp[2 * k + 1];
+        ++w;
+      }
+    }
+    out->offs[c + 1] = (int32_t)w;
+  }
+  free(tmp);
+  return 1;
+}
+
 /* VoronoiMorphoVorPower::dilation (VoronoiVorPower.cpp:24-96). */
 int vo_or_dilate(const vo_or_grid *g, const vo_or_csr *in, double radius, int nthreads,
                  vo_or_csr *out, double *t1_ms, double *t2_ms) {
@@ -503,6 +560,13 @@ int vo_or_dilate(const vo_or_grid *g, const vo_or_csr *in, double radius, int nt
   int rc = tables_build(radius, kmax_of(g), &t);
   if (rc) return rc;
   const int ncols = g->nx * g->ny;
+  vo_or_csr norm = {0};
+  int nrc = normalize_inverted(ncols, in, &norm);
+  if (nrc < 0) {
+    tables_free(&t);
+    return VO_OR_ENOMEM;
+  }
+  if (nrc > 0) in = &norm;
   double t0 = now_ms();
   sep_ctx ctx = {g->nx, g->ny, in, &t, NULL};
   pdriver D1 = {ncols, nthreads, pass1_fn, &ctx, 1, NULL, NULL, NULL, 0};
@@ -511,6 +575,8 @@ int vo_or_dilate(const vo_or_grid *g, const vo_or_csr *in, double radius, int nt
   unsigned char *pd = NULL;
   rc = pdrive(&D1, &poffs, &pv, &pd);
   if (rc) {
+    free(norm.offs);
+    free(norm.z);
     tables_free(&t);
     return rc;
   }
@@ -525,6 +591,8 @@ int vo_or_dilate(const vo_or_grid *g, const vo_or_csr *in, double radius, int nt
   free(poffs);
   free(pv);
   free(pd);
+  free(norm.offs);
+  free(norm.z);
   tables_free(&t);
   return rc;
 }
@@ -647,9 +715,17 @@ int vo_or_dilate_brute(const vo_or_grid *g, const vo_or_csr *in, double radius, 
   tables t;
   int rc = tables_build(radius, kmax_of(g), &t);
   if (rc) return rc;
-  brute_ctx ctx = {g->nx, g->ny, in, &t};
+  vo_or_csr norm = {0};
+  int nrc = normalize_inverted(g->nx * g->ny, in, &norm);
+  if (nrc < 0) {
+    tables_free(&t);
+    return VO_OR_ENOMEM;
+  }
+  brute_ctx ctx = {g->nx, g->ny, nrc > 0 ? &norm : in, &t};
   pdriver D = {g->nx * g->ny, nthreads, brute_fn, &ctx, 0, NULL, NULL, NULL, 0};
   rc = pdrive(&D, &out->offs, &out->z, NULL);
+  free(norm.offs);
+  free(norm.z);
   tables_free(&t);
   return rc;
 }

@@ -25,11 +25,15 @@ def run(ctx, grid, offs, z, op, r, method="separable"):
     return res, t
 
 
+METHODS = ["separable", "fast"]
+
+
 @pytest.mark.parametrize("path", GOLDEN, ids=lambda p: p.split("/")[-1][:-4])
 @pytest.mark.parametrize("op", OPS)
-def test_gpu_matches_reference_golden(ctx, vo, path, op):
+@pytest.mark.parametrize("method", METHODS)
+def test_gpu_matches_reference_golden(ctx, vo, path, op, method):
     grid, d = load_golden(path)
-    got, _ = run(ctx, grid, d["offs"], d["z"], op, float(d["radius"]))
+    got, _ = run(ctx, grid, d["offs"], d["z"], op, float(d["radius"]), method)
     assert_same(got, (d[f"{op}_offs"], d[f"{op}_z"]), tol=1e-9, what=f"{path}:{op}")
 
 
@@ -44,19 +48,21 @@ RADII = [0.0, 1.0, 4.5, 8.0, 16.0, 32.0]
 
 @pytest.mark.parametrize("case", range(len(CASES)))
 @pytest.mark.parametrize("r", RADII)
-def test_gpu_dilation_bit_exact(ctx, vo, oracle, case, r):
+@pytest.mark.parametrize("method", METHODS)
+def test_gpu_dilation_bit_exact(ctx, vo, oracle, case, r, method):
     grid, offs, z = vo.synth_volume(vo.SynthSpec(**CASES[case]))
     want = oracle.morph(ogrid(oracle, grid), offs, z, r, "dilation")
-    got, _ = run(ctx, grid, offs, z, "dilation", r)
+    got, _ = run(ctx, grid, offs, z, "dilation", r, method)
     assert_same(got, want, tol=0.0, what=f"case {case} r={r}")
 
 
 @pytest.mark.parametrize("case", range(len(CASES)))
 @pytest.mark.parametrize("op", ["erosion", "opening", "closing"])
-def test_gpu_chained_ops_bit_exact(ctx, vo, oracle, case, op):
+@pytest.mark.parametrize("method", METHODS)
+def test_gpu_chained_ops_bit_exact(ctx, vo, oracle, case, op, method):
     grid, offs, z = vo.synth_volume(vo.SynthSpec(**CASES[case]))
     want = oracle.morph(ogrid(oracle, grid), offs, z, 6.0, op)
-    got, _ = run(ctx, grid, offs, z, op, 6.0)
+    got, _ = run(ctx, grid, offs, z, op, 6.0, method)
     assert_same(got, want, tol=0.0, what=f"case {case} {op}")
 
 
@@ -70,7 +76,8 @@ def test_gpu_brute_force(ctx, vo, oracle, r):
     assert_same(got, sep, tol=1e-9, what="brute vs separable")
 
 
-def test_gpu_edge_shapes(ctx, vo, oracle):
+@pytest.mark.parametrize("method", METHODS)
+def test_gpu_edge_shapes(ctx, vo, oracle, method):
     rng = np.random.default_rng(5)
     for nx, ny in [(1, 1), (1, 37), (41, 1), (3, 70), (33, 5)]:
         counts = rng.integers(0, 4, size=nx * ny)
@@ -83,11 +90,12 @@ def test_gpu_edge_shapes(ctx, vo, oracle):
         grid = vo.Grid(nx, ny, (0, 0, 0), (nx, ny, 50), 1.0, 0)
         for op in OPS:
             want = oracle.morph(ogrid(oracle, grid), offs, z, 3.5, op)
-            got, _ = run(ctx, grid, offs, z, op, 3.5)
+            got, _ = run(ctx, grid, offs, z, op, 3.5, method)
             assert_same(got, want, tol=0.0, what=f"{nx}x{ny} {op}")
 
 
-def test_gpu_empty_and_full_columns(ctx, vo, oracle):
+@pytest.mark.parametrize("method", METHODS)
+def test_gpu_empty_and_full_columns(ctx, vo, oracle, method):
     nx, ny = 20, 17
     counts = np.zeros(nx * ny, np.int64)
     counts[::7] = 1
@@ -96,14 +104,15 @@ def test_gpu_empty_and_full_columns(ctx, vo, oracle):
     grid = vo.Grid(nx, ny, (0, 0, 0), (nx, ny, 30), 1.0, 0)
     for op in OPS:
         want = oracle.morph(ogrid(oracle, grid), offs, z, 2.5, op)
-        got, _ = run(ctx, grid, offs, z, op, 2.5)
+        got, _ = run(ctx, grid, offs, z, op, 2.5, method)
         assert_same(got, want, tol=0.0, what=op)
     empty = np.zeros(nx * ny + 1, np.int32)
-    got, _ = run(ctx, grid, empty, np.zeros(0), "dilation", 4.0)
+    got, _ = run(ctx, grid, empty, np.zeros(0), "dilation", 4.0, method)
     assert got[0][-1] == 0
 
 
-def test_gpu_zero_length_and_touching_segments(ctx, vo, oracle):
+@pytest.mark.parametrize("method", METHODS)
+def test_gpu_zero_length_and_touching_segments(ctx, vo, oracle, method):
     nx, ny = 24, 24
     rng = np.random.default_rng(8)
     offs = [0]
@@ -120,11 +129,12 @@ def test_gpu_zero_length_and_touching_segments(ctx, vo, oracle):
     grid = vo.Grid(nx, ny, (0, 0, 0), (nx, ny, 40), 1.0, 0)
     for r in [0.0, 1.0, 2.0, 5.0]:  # exact lattice radii produce many exact touches
         want = oracle.morph(ogrid(oracle, grid), offs, z, r, "dilation")
-        got, _ = run(ctx, grid, offs, z, "dilation", r)
+        got, _ = run(ctx, grid, offs, z, "dilation", r, method)
         assert_same(got, want, tol=0.0, what=f"r={r}")
 
 
-def test_gpu_overflow_path(ctx, vo, oracle):
+@pytest.mark.parametrize("method", METHODS)
+def test_gpu_overflow_path(ctx, vo, oracle, method):
     # many thin disjoint plates per column overflow the fast kernels' working
     # lists; the large-capacity re-run must give the same answer
     nx, ny, k = 40, 40, 60
@@ -134,14 +144,15 @@ def test_gpu_overflow_path(ctx, vo, oracle):
     zz = np.tile(z, nx * ny)
     grid = vo.Grid(nx, ny, (0, 0, 0), (nx, ny, 3 * k), 1.0, 0)
     want = oracle.morph(ogrid(oracle, grid), offs, zz, 0.9, "dilation")
-    got, t = run(ctx, grid, offs, zz, "dilation", 0.9)
+    got, t = run(ctx, grid, offs, zz, "dilation", 0.9, method)
     assert t["overflow_columns"] > 0
     assert_same(got, want, tol=0.0)
 
 
 def test_gpu_rejects_bad_input(ctx, vo):
-    grid = vo.Grid(4, 4, (0, 0, 0), (4, 4, 4), 1.0, 0)
-    offs = np.zeros(17, np.int32)
+    # 40 columns wide: x_s + r rounds up to the next integer for x_s >= 7
+    grid = vo.Grid(40, 40, (0, 0, 0), (40, 40, 40), 1.0, 0)
+    offs = np.zeros(1601, np.int32)
     v = ctx.upload(grid, offs, np.zeros(0))
     with pytest.raises(vo.GpuError) as e:
         ctx.morph(v, "dilation", -1.0)
@@ -150,9 +161,15 @@ def test_gpu_rejects_bad_input(ctx, vo):
         ctx.morph(v, "dilation", 3.0 - 1e-15)  # a hair below a lattice distance
     assert e.value.code == vo.VO_ERADIUS
     bad = offs.copy()
-    bad[3] = 5
+    bad[3] = 5  # offsets must not decrease
     with pytest.raises(vo.GpuError):
         ctx.upload(grid, bad, np.zeros(10))
+    import ctypes as C
+    out_h = C.c_void_p()
+    rc = vo.lib().vo_morph(ctx.handle, 0, 99, 2.0, v.handle, C.byref(out_h), None)  # unknown method
+    assert rc == vo.VO_EINVAL and not out_h.value
+    rc = vo.lib().vo_morph(ctx.handle, 7, 0, 2.0, v.handle, C.byref(out_h), None)  # unknown op
+    assert rc == vo.VO_EINVAL
     # the context stays usable after errors
     out, _ = ctx.morph(v, "dilation", 2.0)
     assert out.nseg == 0
@@ -178,3 +195,31 @@ def test_gpu_dexelize_matches_oracle(ctx, vo, oracle):
     got = ctx.download(v)
     assert_same(got, (offs, z), tol=0.0, what="dexelize")
     assert np.all(np.diff(offs) >= 0) and got[0][-1] > 0
+
+
+@pytest.mark.parametrize("method", METHODS + ["brute"])
+def test_gpu_inverted_pairs_normalised(ctx, vo, oracle, method):
+    # columns holding inverted pairs (what negate_ray leaves when values exceed
+    # the complement range) behave as their two endpoints
+    rng = np.random.default_rng(12)
+    nx, ny = 30, 26
+    offs = [0]
+    z = []
+    for c in range(nx * ny):
+        k = int(rng.integers(0, 4))
+        v = np.sort(rng.uniform(0, 40, size=2 * k))
+        pairs = v.reshape(-1, 2).tolist()
+        if pairs and rng.random() < 0.4:
+            a, b = pairs[0]
+            pairs[0] = [b + 0.5, a]  # inverted
+        for a, b in pairs:
+            z += [a, b]
+        offs.append(offs[-1] + len(pairs))
+    offs = np.array(offs, np.int32)
+    z = np.array(z, np.float64)
+    grid = vo.Grid(nx, ny, (0, 0, 0), (nx, ny, 40), 1.0, 0)
+    for r in [2.0, 4.5]:
+        m = "separable" if method == "fast" else method
+        want = oracle.morph(ogrid(oracle, grid), offs, z, r, "dilation", "brute" if method == "brute" else "separable")
+        got, _ = run(ctx, grid, offs, z, "dilation", r, method)
+        assert_same(got, want, tol=0.0, what=f"{method} r={r}")

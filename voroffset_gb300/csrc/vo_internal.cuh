@@ -60,6 +60,9 @@ struct DeviceTables {
 struct vo_volume {
   vo_grid grid;
   int64_t nseg = 0;      // host-known segment count
+  // Whether some pair has z1 > z2 (an inverted pair left by complementing a
+  // column whose values exceed [zmin, zmax]): 0 no, 1 yes, -1 not yet known.
+  mutable int inverted = -1;
   int32_t *offs = nullptr;  // device [nx*ny+1]
   double2 *z = nullptr;     // device [nseg]
   bool owns = true;
@@ -109,6 +112,14 @@ int get_tables(vo_ctx *ctx, double R, int kmax, const DeviceTables **out);
 // is returned through ctx->h_total (synchronising read). Returns VO_ERANGE if
 // the total exceeds INT32_MAX.
 int scan_counts(vo_ctx *ctx, const int32_t *counts, int32_t *offs, int n, long long *total);
+
+// Exact FP32-guarded separable dilation (vo_fast.cu).
+int dilate_fast(vo_ctx *ctx, double R, const vo_volume *in, vo_volume **out, vo_timings *tm);
+
+// Rewrites inverted pairs as their two endpoints (points) and re-sorts / merges
+// the affected columns (vo_morph.cu). *out is a new volume, or nullptr when
+// `in` has no inverted pair.
+int normalize_inverted(vo_ctx *ctx, const vo_volume *in, vo_volume **out);
 
 // Morphology drivers (vo_morph.cu).
 int dilate(vo_ctx *ctx, int method, double R, const vo_volume *in, vo_volume **out,

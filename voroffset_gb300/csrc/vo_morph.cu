@@ -642,6 +642,96 @@ __global__ void k_scan_finish(const long long *__restrict__ tmp, const long long
   if (i == n) offs[n] = ok ? (int32_t)tot : 0;
 }
 
+// ---------------------------------------------------------------- normalisation
+
+// Inverted pairs [a, b], a > b (left by negate_ray on a column whose values
+// exceed [zmin, zmax]) are rewritten as the points [b, b] and [a, a]; such a
+// column is then re-sorted and merged as closed intervals. This is what the
+// reference's power-diagram pass sees of them (SeparatePower2D.cpp:215-226
+// inserts both endpoints as circles).
+constexpr int kNormCap = 64;
+
+__global__ void k_detect_inverted(const double2 *__restrict__ z, int64_t nseg, int *flag) {
+  bool f = false;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nseg; i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 s = z[i];
+    f |= s.x > s.y;
+  }
+  if (__any_sync(0xffffffffu, f) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+}
+
+__device__ int norm_column(const double2 *__restrict__ z, int k0, int k1, double2 *buf, int cap, double2 *out) {
+  bool inv = false;
+  for (int k = k0; k < k1; ++k) inv |= z[k].x > z[k].y;
+  if (!inv) {
+    if (out)
+      for (int k = k0; k < k1; ++k) out[k - k0] = z[k];
+    return k1 - k0;
+  }
+  int n = 0;
+  for (int k = k0; k < k1; ++k) {
+    const double2 s = z[k];
+    double2 parts[2];
+    int np = 0;
+    if (s.x > s.y) {
+      parts[np++] = make_double2(s.y, s.y);
+      parts[np++] = make_double2(s.x, s.x);
+    } else {
+      parts[np++] = s;
+    }
+    for (int q = 0; q < np; ++q) {
+      if (n >= cap) return -1;
+      int i = n++;  // insertion sort by (lo, hi)
+      while (i > 0 && (buf[i - 1].x > parts[q].x || (buf[i - 1].x == parts[q].x && buf[i - 1].y > parts[q].y))) {
+        buf[i] = buf[i - 1];
+        --i;
+      }
+      buf[i] = parts[q];
+    }
+  }
+  int w = 0;
+  for (int i = 0; i < n; ++i) {
+    if (w > 0 && !(buf[w - 1].y < buf[i].x)) {
+      if (buf[i].y > buf[w - 1].y) buf[w - 1].y = buf[i].y;
+    } else {
+      buf[w++] = buf[i];
+    }
+  }
+  if (out)
+    for (int i = 0; i < w; ++i) out[i] = buf[i];
+  return w;
+}
+
+template <bool FILL>
+__global__ void k_norm(int ncols, const int32_t *__restrict__ offs, const double2 *__restrict__ z,
+                       int32_t *counts, const int32_t *ooffs, double2 *oz, OvfList ovf) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncols) return;
+  double2 buf[kNormCap];
+  const int n = norm_column(z, offs[c], offs[c + 1], buf, kNormCap, FILL ? oz + ooffs[c] : nullptr);
+  if (!FILL) {
+    if (n < 0) {
+      record_overflow(ovf, c);
+      counts[c] = 0;
+    } else {
+      counts[c] = n;
+    }
+  }
+}
+
+template <bool FILL>
+__global__ void k_norm_big(const int32_t *__restrict__ offs, const double2 *__restrict__ z, int32_t *counts,
+                           const int32_t *ooffs, double2 *oz, OvfList ovf, double2 *scratch) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+  double2 *buf = scratch + (size_t)tid * 2 * kCapLarge;
+  for (int i = tid; i < *ovf.count; i += nth) {
+    const int c = ovf.cols[i];
+    const int n = norm_column(z, offs[c], offs[c + 1], buf, 2 * kCapLarge, FILL ? oz + ooffs[c] : nullptr);
+    if (n < 0) *ovf.fatal = 1;
+    if (!FILL) counts[c] = n < 0 ? 0 : n;
+  }
+}
+
 }  // namespace
 
 // ================================================================ host side
@@ -715,17 +805,82 @@ int check_fatal(vo_ctx *ctx) {
 
 }  // namespace
 
-int dilate(vo_ctx *ctx, int method, double R, const vo_volume *in, vo_volume **out,
+int normalize_inverted(vo_ctx *ctx, const vo_volume *in, vo_volume **out) {
+  *out = nullptr;
+  if (in->inverted == 0 || in->nseg == 0) {
+    in->inverted = 0;
+    return VO_OK;
+  }
+  if (in->inverted < 0) {
+    int h = 0;
+    VO_CK(ctx, cudaMemsetAsync(ctx->d_flags + 2, 0, sizeof(int), ctx->stream));
+    const int grid = (int)std::min<int64_t>((in->nseg + 255) / 256, 152 * 16);
+    k_detect_inverted<<<grid, 256, 0, ctx->stream>>>(in->z, in->nseg, ctx->d_flags + 2);
+    ctx->launches += 1;
+    VO_CK(ctx, cudaMemcpyAsync(&h, ctx->d_flags + 2, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    VO_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    in->inverted = h ? 1 : 0;
+    if (!h) return VO_OK;
+  }
+  const int ncols = in->grid.nx * in->grid.ny;
+  Scratch s;
+  int rc = alloc_scratch(ctx, ncols, s);
+  if (rc) return rc;
+  OvfList ovf{ctx->d_flags, s.ovf_cols, ctx->d_flags + 1};
+  vo_volume *res = nullptr;
+  long long total = 0;
+  const int gbig = big_grid();
+  cudaMemsetAsync(ctx->d_flags, 0, 2 * sizeof(int), ctx->stream);
+  k_norm<false><<<(ncols + 127) / 128, 128, 0, ctx->stream>>>(ncols, in->offs, in->z, s.counts, nullptr, nullptr,
+                                                              ovf);
+  k_norm_big<false><<<gbig, kBigThreads, 0, ctx->stream>>>(in->offs, in->z, s.counts, nullptr, nullptr, ovf, s.big);
+  ctx->launches += 2;
+  rc = volume_alloc(ctx, in->grid, 0, &res);
+  if (!rc) rc = scan_counts(ctx, s.counts, res->offs, ncols, &total);
+  if (!rc) {
+    res->nseg = total;
+    rc = dalloc(ctx, &res->z, (size_t)total);
+  }
+  if (!rc) {
+    k_norm<true><<<(ncols + 127) / 128, 128, 0, ctx->stream>>>(ncols, in->offs, in->z, nullptr, res->offs, res->z,
+                                                               ovf);
+    k_norm_big<true><<<gbig, kBigThreads, 0, ctx->stream>>>(in->offs, in->z, nullptr, res->offs, res->z, ovf, s.big);
+    ctx->launches += 2;
+    rc = check_fatal(ctx);
+  }
+  free_scratch(ctx, s);
+  if (rc) {
+    if (res) vo_volume_free(ctx, res);
+    return rc;
+  }
+  res->inverted = 0;
+  *out = res;
+  return VO_OK;
+}
+
+int dilate(vo_ctx *ctx, int method, double R, const vo_volume *in_user, vo_volume **out,
            vo_timings *tm) {
+  vo_volume *norm = nullptr;
+  int nrc = normalize_inverted(ctx, in_user, &norm);
+  if (nrc) return nrc;
+  const vo_volume *in = norm ? norm : in_user;
+  if (method == VO_METHOD_FAST) {
+    nrc = dilate_fast(ctx, R, in, out, tm);
+    if (norm) vo_volume_free(ctx, norm);
+    if (!nrc) (*out)->inverted = 0;
+    return nrc;
+  }
   const vo_grid g = in->grid;
   const int nx = g.nx, ny = g.ny, ncols = nx * ny;
   const DeviceTables *T = nullptr;
   int rc = get_tables(ctx, R, std::max(nx, ny), &T);
-  if (rc) return rc;
-  const DevTables t = T->view();
   Scratch s;
-  rc = alloc_scratch(ctx, ncols, s);
-  if (rc) return rc;
+  if (!rc) rc = alloc_scratch(ctx, ncols, s);
+  if (rc) {
+    if (norm) vo_volume_free(ctx, norm);
+    return rc;
+  }
+  const DevTables t = T->view();
   OvfList ovf{ctx->d_flags, s.ovf_cols, ctx->d_flags + 1};
   const dim3 blk(kBX, kBY), grd((nx + kBX - 1) / kBX, (ny + kBY - 1) / kBY);
   const int gbig = big_grid();
@@ -737,6 +892,7 @@ int dilate(vo_ctx *ctx, int method, double R, const vo_volume *in, vo_volume **o
     const size_t shb = sizeof(double) * (size_t)(t.Dy + 1) * (t.Dy + 1);
     if (shb > 200 * 1024) {
       free_scratch(ctx, s);
+      if (norm) vo_volume_free(ctx, norm);
       return set_error(ctx, VO_EINVAL, "brute force supports radius < 160");
     }
     cudaFuncSetAttribute(k_brute<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shb);
@@ -851,11 +1007,13 @@ int dilate(vo_ctx *ctx, int method, double R, const vo_volume *in, vo_volume **o
     dfree(ctx, pd);
   }
   free_scratch(ctx, s);
+  if (norm) vo_volume_free(ctx, norm);
   if (rc) {
     if (res) vo_volume_free(ctx, res);
     return rc;
   }
   VO_CK(ctx, cudaGetLastError());
+  res->inverted = 0;
   *out = res;
   return VO_OK;
 }
