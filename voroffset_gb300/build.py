@@ -20,6 +20,8 @@ import sys
 PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
+HOST = os.path.join(PKG, "host")
+BIN = os.path.join(PKG, "bin")
 BUILD = os.path.join(PKG, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 LIB = os.path.join(PKG, "libvoroffset_gpu.so")
@@ -34,13 +36,15 @@ def _nvcc() -> str:
 
 
 def sources():
-    cu = sorted(f for f in os.listdir(CSRC) if f.endswith(".cu"))
-    cpp = sorted(f for f in os.listdir(CSRC) if f.endswith(".cpp"))
+    cu = sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
+    cpp = sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cpp"))
+    cpp.append(os.path.join(HOST, "voroffset_host.cpp"))
     return cu, cpp
 
 
 def _deps():
     hdrs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
+    hdrs += [os.path.join(HOST, f) for f in os.listdir(HOST) if f.endswith(".h")]
     hdrs += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]
     return max((os.path.getmtime(h) for h in hdrs), default=0.0)
 
@@ -60,21 +64,20 @@ def build(force: bool = False, verbose: bool = False) -> str:
     cu, cpp = sources()
     hdr_time = _deps()
     jobs, objs = [], []
-    for f in cu:
-        src = os.path.join(CSRC, f)
-        obj = os.path.join(BUILD, f + ".o")
+    for src in cu:
+        obj = os.path.join(BUILD, os.path.basename(src) + ".o")
         objs.append(obj)
         if force or not os.path.exists(obj) or os.path.getmtime(obj) < max(os.path.getmtime(src), hdr_time):
             jobs.append([nvcc, ARCH, "-lineinfo", "-O3", "-std=c++17", "--fmad=false", "-Xptxas=-v",
                          "-Xcompiler=-fPIC,-ffp-contract=off", f"-I{INCLUDE}", f"-I{CSRC}", "-c", src,
                          "-o", obj])
-    for f in cpp:
-        src = os.path.join(CSRC, f)
-        obj = os.path.join(BUILD, f + ".o")
+    for src in cpp:
+        obj = os.path.join(BUILD, os.path.basename(src) + ".o")
         objs.append(obj)
         if force or not os.path.exists(obj) or os.path.getmtime(obj) < max(os.path.getmtime(src), hdr_time):
             jobs.append(["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-pthread",
-                         f"-I{INCLUDE}", f"-I{CSRC}", "-I/usr/local/cuda/include", "-c", src, "-o", obj])
+                         f"-I{INCLUDE}", f"-I{CSRC}", f"-I{HOST}", "-I/usr/local/cuda/include", "-c", src,
+                         "-o", obj])
     logs = []
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
@@ -86,6 +89,12 @@ def build(force: bool = False, verbose: bool = False) -> str:
         tmp = LIB + ".tmp"
         _compile([nvcc, ARCH, "-shared", "-o", tmp] + objs + ["-lpthread"], verbose)
         os.replace(tmp, LIB)
+    cli = os.path.join(BIN, "offset3d_gpu")
+    cli_src = os.path.join(HOST, "offset3d_gpu.cpp")
+    if not os.path.exists(cli) or os.path.getmtime(cli) < max(os.path.getmtime(LIB), os.path.getmtime(cli_src)):
+        os.makedirs(BIN, exist_ok=True)
+        _compile(["g++", "-std=c++17", "-O2", f"-I{INCLUDE}", f"-I{HOST}", cli_src, "-o", cli, f"-L{PKG}",
+                  "-lvoroffset_gpu", "-Wl,-rpath,$ORIGIN/..", "-pthread"], verbose)
     return LIB
 
 

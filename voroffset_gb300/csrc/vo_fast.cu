@@ -73,15 +73,21 @@ __device__ __forceinline__ bool lt(const FastArgs &A, float E, float xf, Ids xi,
   return lt_exact(A, xi, px, yi, py);
 }
 
-struct Union {
-  float lo[kKA], hi[kKA];
+// The union of one output column: FP32 endpoint values in shared memory
+// (hot: read by every candidate), laid out [k][thread] so that each lane's
+// bank depends only on its thread index; identities in local memory (touched
+// only when an interval changes, on guard-band ties and for the output).
+struct UnionIds {
   int li[kKA], hi_i[kKA];
   int lda[kKA], hda[kKA];
 };
 
-template <bool FILL>
-__device__ int fast_column(const FastArgs &A, float E, int x, int y, Union &U, double2 *out) {
+// Returns the number of intervals, or -1 when more than kKA are needed.
+// Writes the exact FP64 union to out[0..n).
+__device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv, int stride, UnionIds &U,
+                           double2 *out) {
   int n = 0;
+#define SV(k) sv[(k) * stride]
   for (int p = 0; p < A.npairs; ++p) {
     const int2 ad = A.pairs[p];
     const int a = ad.x, d = ad.y;
@@ -101,25 +107,29 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, Union &U, d
         const float lo = zf.x - h, hi = zf.y + h;
         const Ids il{2 * k, da}, ih{2 * k + 1, da};
         // skip union intervals that end strictly below the candidate
-        while (cur < n && lt(A, E, U.hi[cur], Ids{U.hi_i[cur], U.hda[cur]}, true, lo, il, false)) ++cur;
+        float2 cv = cur < n ? SV(cur) : make_float2(0.f, 0.f);
+        while (cur < n && lt(A, E, cv.y, Ids{U.hi_i[cur], U.hda[cur]}, true, lo, il, false)) {
+          ++cur;
+          if (cur < n) cv = SV(cur);
+        }
         if (cur < n) {
-          const bool lo_in = !lt(A, E, lo, il, false, U.lo[cur], Ids{U.li[cur], U.lda[cur]}, false);
-          const bool hi_in = !lt(A, E, U.hi[cur], Ids{U.hi_i[cur], U.hda[cur]}, true, hi, ih, true);
+          // fast accept: the candidate lies inside U[cur] by more than the guard
+          if (lo - cv.x > E && cv.y - hi > E) continue;
+          const bool lo_in = !lt(A, E, lo, il, false, cv.x, Ids{U.li[cur], U.lda[cur]}, false);
+          const bool hi_in = !lt(A, E, cv.y, Ids{U.hi_i[cur], U.hda[cur]}, true, hi, ih, true);
           if (lo_in && hi_in) continue;  // already covered
         }
-        if (cur == n || lt(A, E, hi, ih, true, U.lo[cur], Ids{U.li[cur], U.lda[cur]}, false)) {
+        if (cur == n || lt(A, E, hi, ih, true, cv.x, Ids{U.li[cur], U.lda[cur]}, false)) {
           // disjoint: insert before cur
           if (n >= kKA) return -1;
           for (int j = n; j > cur; --j) {
-            U.lo[j] = U.lo[j - 1];
-            U.hi[j] = U.hi[j - 1];
+            SV(j) = SV(j - 1);
             U.li[j] = U.li[j - 1];
             U.hi_i[j] = U.hi_i[j - 1];
             U.lda[j] = U.lda[j - 1];
             U.hda[j] = U.hda[j - 1];
           }
-          U.lo[cur] = lo;
-          U.hi[cur] = hi;
+          SV(cur) = make_float2(lo, hi);
           U.li[cur] = il.idx;
           U.hi_i[cur] = ih.idx;
           U.lda[cur] = da;
@@ -128,21 +138,22 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, Union &U, d
           continue;
         }
         // overlapping or touching U[cur]: extend it
-        if (lt(A, E, lo, il, false, U.lo[cur], Ids{U.li[cur], U.lda[cur]}, false)) {
-          U.lo[cur] = lo;
+        if (lt(A, E, lo, il, false, cv.x, Ids{U.li[cur], U.lda[cur]}, false)) {
+          cv.x = lo;
           U.li[cur] = il.idx;
           U.lda[cur] = da;
         }
-        if (lt(A, E, U.hi[cur], Ids{U.hi_i[cur], U.hda[cur]}, true, hi, ih, true)) {
-          U.hi[cur] = hi;
+        if (lt(A, E, cv.y, Ids{U.hi_i[cur], U.hda[cur]}, true, hi, ih, true)) {
+          cv.y = hi;
           U.hi_i[cur] = ih.idx;
           U.hda[cur] = da;
           // absorb following intervals that now start at or below the new end
           int j = cur + 1;
-          while (j < n &&
-                 !lt(A, E, U.hi[cur], Ids{U.hi_i[cur], U.hda[cur]}, true, U.lo[j], Ids{U.li[j], U.lda[j]}, false)) {
-            if (lt(A, E, U.hi[cur], Ids{U.hi_i[cur], U.hda[cur]}, true, U.hi[j], Ids{U.hi_i[j], U.hda[j]}, true)) {
-              U.hi[cur] = U.hi[j];
+          while (j < n) {
+            const float2 nv = SV(j);
+            if (lt(A, E, cv.y, Ids{U.hi_i[cur], U.hda[cur]}, true, nv.x, Ids{U.li[j], U.lda[j]}, false)) break;
+            if (lt(A, E, cv.y, Ids{U.hi_i[cur], U.hda[cur]}, true, nv.y, Ids{U.hi_i[j], U.hda[j]}, true)) {
+              cv.y = nv.y;
               U.hi_i[cur] = U.hi_i[j];
               U.hda[cur] = U.hda[j];
             }
@@ -151,8 +162,7 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, Union &U, d
           const int gone = j - cur - 1;
           if (gone > 0) {
             for (int m = cur + 1; m + gone < n; ++m) {
-              U.lo[m] = U.lo[m + gone];
-              U.hi[m] = U.hi[m + gone];
+              SV(m) = SV(m + gone);
               U.li[m] = U.li[m + gone];
               U.hi_i[m] = U.hi_i[m + gone];
               U.lda[m] = U.lda[m + gone];
@@ -161,33 +171,47 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, Union &U, d
             n -= gone;
           }
         }
+        SV(cur) = cv;
       }
     }
   }
-  if (FILL)
-    for (int k = 0; k < n; ++k)
-      out[k] = make_double2(exact_val(A, U.li[k], U.lda[k], false), exact_val(A, U.hi_i[k], U.hda[k], true));
+#undef SV
+  for (int k = 0; k < n; ++k)
+    out[k] = make_double2(exact_val(A, U.li[k], U.lda[k], false), exact_val(A, U.hi_i[k], U.hda[k], true));
   return n;
 }
 
-template <bool FILL>
-__global__ void __launch_bounds__(kFB *kFBY) k_fast(FastArgs A, int32_t *counts, const int32_t *ooffs,
-                                                    double2 *oz, int *ovf_count, int *ovf_cols) {
+// One pass: the exact union of every output column goes to its fixed-capacity
+// staging slot (kKA intervals) with its count; columns that need more are
+// listed for the FP64 re-run. A compaction pass then packs the slots.
+__global__ void __launch_bounds__(kFB *kFBY) k_fast(FastArgs A, int32_t *counts, double2 *staging,
+                                                    int *ovf_count, int *ovf_cols) {
+  __shared__ float2 sv[kKA * kFB * kFBY];
+  const int tid = threadIdx.x + kFB * threadIdx.y;
   const int x = blockIdx.x * kFB + threadIdx.x;
   const int y = blockIdx.y * kFBY + threadIdx.y;
   if (x >= A.nx || y >= A.ny) return;
   const int c = x + A.nx * y;
   const float E = *A.E;
-  Union U;
-  const int n = fast_column<FILL>(A, E, x, y, U, FILL ? oz + ooffs[c] : nullptr);
-  if (!FILL) {
-    if (n < 0) {
-      ovf_cols[atomicAdd(ovf_count, 1)] = c;
-      counts[c] = 0;
-    } else {
-      counts[c] = n;
-    }
+  UnionIds U;
+  const int n = fast_column(A, E, x, y, sv + tid, kFB * kFBY, U, staging + (size_t)c * kKA);
+  if (n < 0) {
+    ovf_cols[atomicAdd(ovf_count, 1)] = c;
+    counts[c] = 0;
+  } else {
+    counts[c] = n;
   }
+}
+
+// Packs the staging slots of non-overflowing columns into the CSR output.
+__global__ void k_compact(int ncols, const int32_t *__restrict__ counts, const double2 *__restrict__ staging,
+                          const int32_t *__restrict__ ooffs, double2 *__restrict__ oz) {
+  // one warp per column, lanes over intervals
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w >= ncols) return;
+  const int n = ooffs[w + 1] - ooffs[w];
+  if (n > kKA) return;  // written by the FP64 re-run
+  for (int k = lane; k < n; k += 32) oz[ooffs[w] + k] = staging[(size_t)w * kKA + k];
 }
 
 // FP64 re-run of columns whose union outgrew kKA: same candidate set, exact
@@ -355,9 +379,11 @@ int dilate_fast(vo_ctx *ctx, double R, const vo_volume *in, vo_volume **out, vo_
   }
   FastArgs A{nx, ny, h.W, in->offs, (const double *)in->z, zf, T->Hf, T->H, dpairs, (int)pairs.size(), dE};
   const dim3 blk(kFB, kFBY), grd((nx + kFB - 1) / kFB, (ny + kFBY - 1) / kFBY);
+  double2 *staging = nullptr;
+  if (!rc) rc = dalloc(ctx, &staging, (size_t)ncols * kKA);
   if (!rc) {
     cudaEventRecord(ctx->ev[4], ctx->stream);
-    k_fast<false><<<grd, blk, 0, ctx->stream>>>(A, counts, nullptr, nullptr, ctx->d_flags, ovf_cols);
+    k_fast<<<grd, blk, 0, ctx->stream>>>(A, counts, staging, ctx->d_flags, ovf_cols);
     k_fast_big<false><<<gbig, kBigThreads, 0, ctx->stream>>>(A, counts, nullptr, nullptr, ctx->d_flags, ovf_cols,
                                                              big, ctx->d_flags + 1);
     ctx->launches += 2;
@@ -371,7 +397,8 @@ int dilate_fast(vo_ctx *ctx, double R, const vo_volume *in, vo_volume **out, vo_
   }
   if (!rc) {
     cudaEventRecord(ctx->ev[6], ctx->stream);
-    k_fast<true><<<grd, blk, 0, ctx->stream>>>(A, nullptr, res->offs, res->z, ctx->d_flags, ovf_cols);
+    k_compact<<<(int)(((int64_t)ncols * 32 + 255) / 256), 256, 0, ctx->stream>>>(ncols, counts, staging, res->offs,
+                                                                                 res->z);
     k_fast_big<true><<<gbig, kBigThreads, 0, ctx->stream>>>(A, nullptr, res->offs, res->z, ctx->d_flags, ovf_cols,
                                                             big, ctx->d_flags + 1);
     ctx->launches += 2;
@@ -386,6 +413,7 @@ int dilate_fast(vo_ctx *ctx, double R, const vo_volume *in, vo_volume **out, vo_
     else
       ctx->ovf_cols += hf[0];
   }
+  dfree(ctx, staging);
   if (!rc && tm) {
     float e0 = 0, e1 = 0, e2 = 0;
     cudaEventElapsedTime(&e0, ctx->ev[0], ctx->ev[1]);
