@@ -47,9 +47,11 @@ struct FastArgs {
   const float *E;       // guard band (device scalar)
 };
 
-struct Ids {
-  int idx;  // index into zd
-  int da;   // d | a << 8
+// Identities of union endpoints, kept in local memory and read only when an
+// FP32 comparison falls inside the guard band or the output is written.
+struct UnionIds {
+  int li[kKA], hi_i[kKA];  // input value index of the lower / upper endpoint
+  int lda[kKA], hda[kKA];  // d | a << 8 of the lower / upper endpoint
 };
 
 __device__ __forceinline__ double exact_val(const FastArgs &A, int idx, int da, bool plus) {
@@ -58,29 +60,28 @@ __device__ __forceinline__ double exact_val(const FastArgs &A, int idx, int da, 
   return plus ? __dadd_rn(z, h) : __dsub_rn(z, h);
 }
 
-__device__ __noinline__ bool lt_exact(const FastArgs &A, Ids xi, bool px, Ids yi, bool py) {
-  return exact_val(A, xi.idx, xi.da, px) < exact_val(A, yi.idx, yi.da, py);
+// Exact comparisons, out of line: identities are loaded only here.
+// Union endpoint (j, hi?) < candidate endpoint (idx, da, plus)?
+__device__ __noinline__ bool ex_u_lt_c(const FastArgs &A, const UnionIds &U, int j, bool jhi, int idx, int da,
+                                       bool plus) {
+  const double u = jhi ? exact_val(A, U.hi_i[j], U.hda[j], true) : exact_val(A, U.li[j], U.lda[j], false);
+  return u < exact_val(A, idx, da, plus);
+}
+// Candidate endpoint < union endpoint?
+__device__ __noinline__ bool ex_c_lt_u(const FastArgs &A, const UnionIds &U, int idx, int da, bool plus, int j,
+                                       bool jhi) {
+  const double u = jhi ? exact_val(A, U.hi_i[j], U.hda[j], true) : exact_val(A, U.li[j], U.lda[j], false);
+  return exact_val(A, idx, da, plus) < u;
+}
+// Union endpoint (i, ihi) < union endpoint (j, jhi)?
+__device__ __noinline__ bool ex_u_lt_u(const FastArgs &A, const UnionIds &U, int i, bool ihi, int j, bool jhi) {
+  const double a = ihi ? exact_val(A, U.hi_i[i], U.hda[i], true) : exact_val(A, U.li[i], U.lda[i], false);
+  const double b = jhi ? exact_val(A, U.hi_i[j], U.hda[j], true) : exact_val(A, U.li[j], U.lda[j], false);
+  return a < b;
 }
 
-// x < y for two candidate endpoints given their FP32 approximations and
-// identities (px / py: whether the endpoint is a z2 + H "upper" value).
-// Decided in FP32 outside the guard band, exactly in FP64 inside it.
-__device__ __forceinline__ bool lt(const FastArgs &A, float E, float xf, Ids xi, bool px, float yf,
-                                   Ids yi, bool py) {
-  const float t = yf - xf;
-  if (t > E) return true;
-  if (t < -E) return false;
-  return lt_exact(A, xi, px, yi, py);
-}
-
-// The union of one output column: FP32 endpoint values in shared memory
-// (hot: read by every candidate), laid out [k][thread] so that each lane's
-// bank depends only on its thread index; identities in local memory (touched
-// only when an interval changes, on guard-band ties and for the output).
-struct UnionIds {
-  int li[kKA], hi_i[kKA];
-  int lda[kKA], hda[kKA];
-};
+// FP32 difference t = y - x decides x < y outside the guard band [-E, E].
+#define GUARD(t, E, exact) ((t) > (E) ? true : ((t) < -(E) ? false : (exact)))
 
 // Returns the number of intervals, or -1 when more than kKA are needed.
 // Writes the exact FP64 union to out[0..n).
@@ -102,24 +103,22 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
       const int c = xs + A.nx * ys;
       const int k0 = A.offs[c], k1 = A.offs[c + 1];
       int cur = 0;
+      float2 cv = n > 0 ? SV(0) : make_float2(0.f, 0.f);
       for (int k = k0; k < k1; ++k) {
         const float2 zf = *reinterpret_cast<const float2 *>(A.zf + 2 * k);
         const float lo = zf.x - h, hi = zf.y + h;
-        const Ids il{2 * k, da}, ih{2 * k + 1, da};
-        // skip union intervals that end strictly below the candidate
-        float2 cv = cur < n ? SV(cur) : make_float2(0.f, 0.f);
-        while (cur < n && lt(A, E, cv.y, Ids{U.hi_i[cur], U.hda[cur]}, true, lo, il, false)) {
+        const int il = 2 * k, ih = 2 * k + 1;
+        // skip union intervals that end strictly below the candidate: U.hi[cur] < lo
+        while (cur < n && GUARD(lo - cv.y, E, ex_u_lt_c(A, U, cur, true, il, da, false))) {
           ++cur;
           if (cur < n) cv = SV(cur);
         }
         if (cur < n) {
-          // fast accept: the candidate lies inside U[cur] by more than the guard
-          if (lo - cv.x > E && cv.y - hi > E) continue;
-          const bool lo_in = !lt(A, E, lo, il, false, cv.x, Ids{U.li[cur], U.lda[cur]}, false);
-          const bool hi_in = !lt(A, E, cv.y, Ids{U.hi_i[cur], U.hda[cur]}, true, hi, ih, true);
-          if (lo_in && hi_in) continue;  // already covered
+          // covered: U.lo[cur] <= lo and hi <= U.hi[cur]
+          const bool lo_in = !GUARD(cv.x - lo, E, ex_c_lt_u(A, U, il, da, false, cur, false));
+          if (lo_in && !GUARD(hi - cv.y, E, ex_u_lt_c(A, U, cur, true, ih, da, true))) continue;
         }
-        if (cur == n || lt(A, E, hi, ih, true, cv.x, Ids{U.li[cur], U.lda[cur]}, false)) {
+        if (cur == n || GUARD(cv.x - hi, E, ex_c_lt_u(A, U, ih, da, true, cur, false))) {
           // disjoint: insert before cur
           if (n >= kKA) return -1;
           for (int j = n; j > cur; --j) {
@@ -129,30 +128,31 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
             U.lda[j] = U.lda[j - 1];
             U.hda[j] = U.hda[j - 1];
           }
-          SV(cur) = make_float2(lo, hi);
-          U.li[cur] = il.idx;
-          U.hi_i[cur] = ih.idx;
+          cv = make_float2(lo, hi);
+          SV(cur) = cv;
+          U.li[cur] = il;
+          U.hi_i[cur] = ih;
           U.lda[cur] = da;
           U.hda[cur] = da;
           ++n;
           continue;
         }
         // overlapping or touching U[cur]: extend it
-        if (lt(A, E, lo, il, false, cv.x, Ids{U.li[cur], U.lda[cur]}, false)) {
+        if (GUARD(cv.x - lo, E, ex_c_lt_u(A, U, il, da, false, cur, false))) {
           cv.x = lo;
-          U.li[cur] = il.idx;
+          U.li[cur] = il;
           U.lda[cur] = da;
         }
-        if (lt(A, E, cv.y, Ids{U.hi_i[cur], U.hda[cur]}, true, hi, ih, true)) {
+        if (GUARD(hi - cv.y, E, ex_u_lt_c(A, U, cur, true, ih, da, true))) {
           cv.y = hi;
-          U.hi_i[cur] = ih.idx;
+          U.hi_i[cur] = ih;
           U.hda[cur] = da;
           // absorb following intervals that now start at or below the new end
           int j = cur + 1;
           while (j < n) {
             const float2 nv = SV(j);
-            if (lt(A, E, cv.y, Ids{U.hi_i[cur], U.hda[cur]}, true, nv.x, Ids{U.li[j], U.lda[j]}, false)) break;
-            if (lt(A, E, cv.y, Ids{U.hi_i[cur], U.hda[cur]}, true, nv.y, Ids{U.hi_i[j], U.hda[j]}, true)) {
+            if (GUARD(nv.x - cv.y, E, ex_u_lt_u(A, U, cur, true, j, false))) break;  // U.hi[cur] < U.lo[j]
+            if (GUARD(nv.y - cv.y, E, ex_u_lt_u(A, U, cur, true, j, true))) {       // U.hi[cur] < U.hi[j]
               cv.y = nv.y;
               U.hi_i[cur] = U.hi_i[j];
               U.hda[cur] = U.hda[j];
