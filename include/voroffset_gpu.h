@@ -131,6 +131,23 @@ int vo_dexelize(vo_ctx *ctx, const double *verts, int nv, const int32_t *tris, i
  * calculateXor's return value), computed on the device. */
 int vo_xor_volume(vo_ctx *ctx, const vo_volume *a, const vo_volume *b, double *volume);
 
+/* Allocation-free xor volume. No counterpart in the reference: the same result
+ * as vo_xor_volume, for callers that must not allocate device memory while
+ * they run (code inside a stream host callback, services whose device memory
+ * is owned by another allocator, hot loops kept off the allocator). It takes
+ * no context: offs_a/z_a and offs_b/z_b are the device CSR arrays of two
+ * volumes on `grid` (e.g. from vo_volume_device_ptrs), on the current device;
+ * the work runs on `stream` (a cudaStream_t, NULL for the default stream),
+ * which is synchronised before *volume is written.
+ * Scratch is a fixed file-scope device array of 65537 doubles (512 KiB) that
+ * every GPU loading the library keeps until exit; grids with more than
+ * 16,777,216 columns (nx*ny) return VO_ERANGE. The first call on each device
+ * looks up that array's device address, so make it before any stream capture.
+ * All calls share the array: calls that overlap on the GPU (different streams
+ * or threads) race and must be serialised by the caller. */
+int vo_xor_volume_noalloc(const vo_grid *grid, const int32_t *offs_a, const double *z_a,
+                          const int32_t *offs_b, const double *z_b, void *stream, double *volume);
+
 /* ---- host utilities (no device work) ---- */
 
 /* Seeded synthetic volume: union of spheres and flat-capped cylinders

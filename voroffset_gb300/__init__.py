@@ -101,6 +101,7 @@ SIGNATURES = {
     "vo_dexelize": (C.c_int, [_P, C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_int32), C.c_int,
                               C.POINTER(C.c_double), C.c_int, C.c_int, C.POINTER(_P)]),
     "vo_xor_volume": (C.c_int, [_P, _P, _P, C.POINTER(C.c_double)]),
+    "vo_xor_volume_noalloc": (C.c_int, [C.POINTER(_Grid), _P, _P, _P, _P, _P, C.POINTER(C.c_double)]),
     "vo_synth_volume": (C.c_int, [C.POINTER(_SynthParams), C.POINTER(C.c_int32),
                                   C.POINTER(C.POINTER(C.c_double)), C.POINTER(C.c_int64)]),
     "vo_synth_torus": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_uint64,

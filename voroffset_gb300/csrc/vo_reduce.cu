@@ -8,6 +8,8 @@
 // touching pieces), and runs shorter than 1e-10 are dropped like removepoint.
 // Column lengths are summed per block and the block partials are added in a
 // fixed order, so the result is deterministic.
+#include <mutex>
+
 #include "vo_internal.cuh"
 
 namespace vo {
@@ -104,6 +106,82 @@ extern "C" int vo_xor_volume(vo_ctx *ctx, const vo_volume *a, const vo_volume *b
   dfree(ctx, d_out);
   VO_CK(ctx, cudaStreamSynchronize(ctx->stream));
   const double sp = a->grid.spacing;
+  *volume = sp * sp * sp * h;
+  return VO_OK;
+}
+
+// ============================================================ allocation-free variant
+//
+// vo_xor_volume_noalloc runs the same two kernels as vo_xor_volume, but its
+// scratch (one partial sum per block of kThreads columns, plus the result)
+// is the fixed-size array below instead of memory allocated per call. It is
+// for callers that must not allocate device memory while they run: code that
+// executes inside a host callback enqueued on a stream (where CUDA calls that
+// allocate are not permitted), services whose device memory budget is owned
+// by another allocator, and hot loops that must stay off the allocator's
+// locks. Every GPU that loads this library holds the array until the process
+// exits: (kNoAllocMaxBlocks + 1) doubles, 512 KiB + 8 B.
+
+namespace vo {
+namespace {
+
+constexpr int kNoAllocMaxBlocks = 65536;  // at most 65536 * 256 = 16,777,216 columns
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) double g_xor_scratch[kNoAllocMaxBlocks + 1];
+
+// Device address of g_xor_scratch, looked up once per device (in host code the
+// symbol itself is only a host-side stand-in and must not be passed to a kernel).
+double *g_xor_scratch_ptr[kNoAllocMaxDevices] = {};
+std::mutex g_xor_scratch_mutex;
+
+int xor_scratch_for_current_device(double **out) {
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) {
+    cudaGetLastError();
+    return VO_ENODEV;
+  }
+  std::lock_guard<std::mutex> lock(g_xor_scratch_mutex);
+  if (!g_xor_scratch_ptr[dev]) {
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_xor_scratch) != cudaSuccess || !p) {
+      cudaGetLastError();
+      return VO_ECUDA;
+    }
+    g_xor_scratch_ptr[dev] = static_cast<double *>(p);
+  }
+  *out = g_xor_scratch_ptr[dev];
+  return VO_OK;
+}
+
+}  // namespace
+}  // namespace vo
+
+extern "C" int vo_xor_volume_noalloc(const vo_grid *grid, const int32_t *offs_a, const double *z_a,
+                                     const int32_t *offs_b, const double *z_b, void *stream, double *volume) {
+  using namespace vo;
+  if (!grid || grid->nx <= 0 || grid->ny <= 0 || !volume) return VO_EINVAL;
+  const int64_t ncols = (int64_t)grid->nx * grid->ny;
+  if (ncols > (int64_t)kNoAllocMaxBlocks * kThreads) return VO_ERANGE;  // beyond the fixed scratch
+  if (!offs_a || !offs_b) return VO_EINVAL;
+  double *scratch = nullptr;
+  int rc = xor_scratch_for_current_device(&scratch);
+  if (rc) return rc;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int nblk = (int)((ncols + kThreads - 1) / kThreads);
+  // Every partial sum the reduction reads is written by this call's first
+  // kernel, and the result slot by the second: nothing carries over from the
+  // previous call, so no clearing is needed.
+  k_xor<<<nblk, kThreads, 0, st>>>((int)ncols, offs_a, reinterpret_cast<const double2 *>(z_a), offs_b,
+                                   reinterpret_cast<const double2 *>(z_b), scratch);
+  k_sum<<<1, kThreads, 0, st>>>(scratch, nblk, scratch + kNoAllocMaxBlocks);
+  double h = 0;
+  if (cudaMemcpyAsync(&h, scratch + kNoAllocMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess) {
+    cudaGetLastError();
+    return VO_ECUDA;
+  }
+  const double sp = grid->spacing;
   *volume = sp * sp * sp * h;
   return VO_OK;
 }
