@@ -85,6 +85,11 @@ __device__ __noinline__ bool ex_u_lt_u(const FastArgs &A, const UnionIds &U, int
 
 // Returns the number of intervals, or -1 when more than kKA are needed.
 // Writes the exact FP64 union to out[0..n).
+//
+// The interval under the cursor is cached in registers (values cv, identities
+// cli/chi/clda/chda) and written back when the cursor moves or a source column
+// ends, so extending it touches no memory. The four source columns of a
+// (|dx|, |dy|) pair share one loop.
 __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv, int stride, UnionIds &U,
                            double2 *out) {
   int n = 0;
@@ -94,86 +99,146 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
     const int a = ad.x, d = ad.y;
     const float h = A.Hf[d * A.W + a];
     const int da = d | (a << 8);
+    // segment ranges of the (up to four) source columns of this pair
+    int kb[4], ke[4];
+#pragma unroll
     for (int s = 0; s < 4; ++s) {
       const int xs = (s & 1) ? x + a : x - a;
       const int ys = (s & 2) ? y + d : y - d;
-      if ((s & 1) && a == 0) continue;
-      if ((s & 2) && d == 0) continue;
-      if (xs < 0 || xs >= A.nx || ys < 0 || ys >= A.ny) continue;
+      const bool ok = !((s & 1) && a == 0) && !((s & 2) && d == 0) && xs >= 0 && xs < A.nx && ys >= 0 &&
+                      ys < A.ny;
       const int c = xs + A.nx * ys;
-      const int k0 = A.offs[c], k1 = A.offs[c + 1];
-      int cur = 0;
-      float2 cv = n > 0 ? SV(0) : make_float2(0.f, 0.f);
-      for (int k = k0; k < k1; ++k) {
-        const float2 zf = *reinterpret_cast<const float2 *>(A.zf + 2 * k);
-        const float lo = zf.x - h, hi = zf.y + h;
-        const int il = 2 * k, ih = 2 * k + 1;
-        // skip union intervals that end strictly below the candidate: U.hi[cur] < lo
-        while (cur < n && GUARD(lo - cv.y, E, ex_u_lt_c(A, U, cur, true, il, da, false))) {
-          ++cur;
-          if (cur < n) cv = SV(cur);
+      kb[s] = ok ? A.offs[c] : 0;
+      ke[s] = ok ? A.offs[c + 1] : 0;
+    }
+    int s = 0, k = kb[0], kend = ke[0];
+    int cur = 0;
+    float2 cv = n > 0 ? SV(0) : make_float2(0.f, 0.f);
+    int cli = 0, chi = 0, clda = 0, chda = 0;  // identities of U[cur] (valid when cached)
+    bool cached = false;                       // cached identities differ from U[cur] in memory
+    bool loaded = false;                       // cli.. hold U[cur]'s identities
+#define LOAD_IDS()                 \
+  if (!loaded) {                   \
+    cli = U.li[cur];               \
+    chi = U.hi_i[cur];             \
+    clda = U.lda[cur];             \
+    chda = U.hda[cur];             \
+    loaded = true;                 \
+  }
+#define FLUSH()                    \
+  if (cached) {                    \
+    U.li[cur] = cli;               \
+    U.hi_i[cur] = chi;             \
+    U.lda[cur] = clda;             \
+    U.hda[cur] = chda;             \
+    SV(cur) = cv;                  \
+    cached = false;                \
+  }
+    for (;;) {
+      while (k >= kend) {
+        // next source column: write back the cached interval, restart the cursor
+        FLUSH();
+        if (++s >= 4) break;
+        k = kb[s];
+        kend = ke[s];
+        cur = 0;
+        loaded = false;
+        if (n > 0) cv = SV(0);
+      }
+      if (s >= 4) break;
+      const float2 zf = *reinterpret_cast<const float2 *>(A.zf + 2 * k);
+      const float lo = zf.x - h, hi = zf.y + h;
+      const int il = 2 * k, ih = 2 * k + 1;
+      ++k;
+      // skip union intervals that end strictly below the candidate: U.hi[cur] < lo
+      while (cur < n) {
+        const float t = lo - cv.y;
+        bool below;
+        if (t > E) {
+          below = true;
+        } else if (t < -E) {
+          below = false;
+        } else {
+          FLUSH();
+          below = ex_u_lt_c(A, U, cur, true, il, da, false);
         }
-        if (cur < n) {
-          // covered: U.lo[cur] <= lo and hi <= U.hi[cur]
-          const bool lo_in = !GUARD(cv.x - lo, E, ex_c_lt_u(A, U, il, da, false, cur, false));
-          if (lo_in && !GUARD(hi - cv.y, E, ex_u_lt_c(A, U, cur, true, ih, da, true))) continue;
+        if (!below) break;
+        FLUSH();
+        ++cur;
+        loaded = false;
+        if (cur < n) cv = SV(cur);
+      }
+      if (cur < n) {
+        // covered: U.lo[cur] <= lo and hi <= U.hi[cur]
+        if (lo - cv.x > E && cv.y - hi > E) continue;  // fast accept
+        FLUSH();
+        const bool lo_in = !GUARD(cv.x - lo, E, ex_c_lt_u(A, U, il, da, false, cur, false));
+        if (lo_in && !GUARD(hi - cv.y, E, ex_u_lt_c(A, U, cur, true, ih, da, true))) continue;
+      }
+      FLUSH();
+      if (cur == n || GUARD(cv.x - hi, E, ex_c_lt_u(A, U, ih, da, true, cur, false))) {
+        // disjoint: insert before cur
+        if (n >= kKA) return -1;
+        for (int j = n; j > cur; --j) {
+          SV(j) = SV(j - 1);
+          U.li[j] = U.li[j - 1];
+          U.hi_i[j] = U.hi_i[j - 1];
+          U.lda[j] = U.lda[j - 1];
+          U.hda[j] = U.hda[j - 1];
         }
-        if (cur == n || GUARD(cv.x - hi, E, ex_c_lt_u(A, U, ih, da, true, cur, false))) {
-          // disjoint: insert before cur
-          if (n >= kKA) return -1;
-          for (int j = n; j > cur; --j) {
-            SV(j) = SV(j - 1);
-            U.li[j] = U.li[j - 1];
-            U.hi_i[j] = U.hi_i[j - 1];
-            U.lda[j] = U.lda[j - 1];
-            U.hda[j] = U.hda[j - 1];
+        cv = make_float2(lo, hi);
+        cli = il;
+        chi = ih;
+        clda = da;
+        chda = da;
+        loaded = true;
+        cached = true;
+        ++n;
+        continue;
+      }
+      // overlapping or touching U[cur]: extend it (in registers)
+      LOAD_IDS();
+      if (GUARD(cv.x - lo, E, ex_c_lt_u(A, U, il, da, false, cur, false))) {
+        cv.x = lo;
+        cli = il;
+        clda = da;
+        cached = true;
+      }
+      if (GUARD(hi - cv.y, E, ex_u_lt_c(A, U, cur, true, ih, da, true))) {
+        cv.y = hi;
+        chi = ih;
+        chda = da;
+        cached = true;
+        // absorb following intervals that now start at or below the new end
+        FLUSH();
+        int j = cur + 1;
+        while (j < n) {
+          const float2 nv = SV(j);
+          if (GUARD(nv.x - cv.y, E, ex_u_lt_u(A, U, cur, true, j, false))) break;  // U.hi[cur] < U.lo[j]
+          if (GUARD(nv.y - cv.y, E, ex_u_lt_u(A, U, cur, true, j, true))) {       // U.hi[cur] < U.hi[j]
+            cv.y = nv.y;
+            U.hi_i[cur] = U.hi_i[j];
+            U.hda[cur] = U.hda[j];
+            SV(cur) = cv;
           }
-          cv = make_float2(lo, hi);
-          SV(cur) = cv;
-          U.li[cur] = il;
-          U.hi_i[cur] = ih;
-          U.lda[cur] = da;
-          U.hda[cur] = da;
-          ++n;
-          continue;
+          ++j;
         }
-        // overlapping or touching U[cur]: extend it
-        if (GUARD(cv.x - lo, E, ex_c_lt_u(A, U, il, da, false, cur, false))) {
-          cv.x = lo;
-          U.li[cur] = il;
-          U.lda[cur] = da;
-        }
-        if (GUARD(hi - cv.y, E, ex_u_lt_c(A, U, cur, true, ih, da, true))) {
-          cv.y = hi;
-          U.hi_i[cur] = ih;
-          U.hda[cur] = da;
-          // absorb following intervals that now start at or below the new end
-          int j = cur + 1;
-          while (j < n) {
-            const float2 nv = SV(j);
-            if (GUARD(nv.x - cv.y, E, ex_u_lt_u(A, U, cur, true, j, false))) break;  // U.hi[cur] < U.lo[j]
-            if (GUARD(nv.y - cv.y, E, ex_u_lt_u(A, U, cur, true, j, true))) {       // U.hi[cur] < U.hi[j]
-              cv.y = nv.y;
-              U.hi_i[cur] = U.hi_i[j];
-              U.hda[cur] = U.hda[j];
-            }
-            ++j;
+        const int gone = j - cur - 1;
+        if (gone > 0) {
+          for (int m = cur + 1; m + gone < n; ++m) {
+            SV(m) = SV(m + gone);
+            U.li[m] = U.li[m + gone];
+            U.hi_i[m] = U.hi_i[m + gone];
+            U.lda[m] = U.lda[m + gone];
+            U.hda[m] = U.hda[m + gone];
           }
-          const int gone = j - cur - 1;
-          if (gone > 0) {
-            for (int m = cur + 1; m + gone < n; ++m) {
-              SV(m) = SV(m + gone);
-              U.li[m] = U.li[m + gone];
-              U.hi_i[m] = U.hi_i[m + gone];
-              U.lda[m] = U.lda[m + gone];
-              U.hda[m] = U.hda[m + gone];
-            }
-            n -= gone;
-          }
+          n -= gone;
         }
-        SV(cur) = cv;
+        loaded = false;
       }
     }
+#undef LOAD_IDS
+#undef FLUSH
   }
 #undef SV
   for (int k = 0; k < n; ++k)
