@@ -345,9 +345,19 @@ int vo_morph(vo_ctx *ctx, int op, int method, double radius, const vo_volume *in
 int vo_morph_batched(vo_ctx *ctx, int n, const int *ops, const double *radii, int method,
                      const vo_volume *const *ins, vo_volume **outs, vo_timings *tm) {
   if (!ctx || n < 0 || (n > 0 && (!ops || !radii || !ins || !outs))) return VO_EINVAL;
+  for (int i = 0; i < n; ++i) outs[i] = nullptr;
+  if (method == VO_METHOD_FAST) {
+    for (int i = 0; i < n; ++i) {
+      if (!ins[i] || ops[i] < VO_DILATION || ops[i] > VO_CLOSING || !(radii[i] >= 0) || radii[i] > 255)
+        return set_error(ctx, VO_EINVAL, "morph_batched: bad volume, op or radius");
+    }
+    cudaSetDevice(ctx->device);
+    ctx->err.clear();
+    ctx->launches = 0;
+    return morph_batched_fast(ctx, n, ops, radii, ins, outs, tm);
+  }
   vo_timings acc;
   std::memset(&acc, 0, sizeof acc);
-  for (int i = 0; i < n; ++i) outs[i] = nullptr;
   for (int i = 0; i < n; ++i) {
     vo_timings t;
     int rc = vo_morph(ctx, ops[i], method, radii[i], ins[i], &outs[i], &t);

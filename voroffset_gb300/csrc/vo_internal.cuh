@@ -127,6 +127,29 @@ int dilate(vo_ctx *ctx, int method, double R, const vo_volume *in, vo_volume **o
 int erode(vo_ctx *ctx, int method, double R, const vo_volume *in, vo_volume **out,
           vo_timings *tm);
 
+// Fixed-capacity slot volume: column c at z[c*cap, end[c]), beg[c] = c*cap;
+// a CSR volume is viewed as one with beg = offs, end = offs + 1.
+struct SlotVol {
+  vo_grid grid{};
+  int cap = 0;
+  int32_t *beg = nullptr, *end = nullptr;
+  double2 *z = nullptr;
+  bool owns = false;
+};
+int slot_alloc(vo_ctx *ctx, const vo_grid &g, int cap, SlotVol &v);
+void slot_free(vo_ctx *ctx, SlotVol &v);
+SlotVol slot_view(const vo_volume *in, int cap);
+void slot_end_from_counts(vo_ctx *ctx, SlotVol &v, const int32_t *counts);
+int slot_negate(vo_ctx *ctx, const SlotVol &in, SlotVol &out, int *overflow);
+int slot_normalize(vo_ctx *ctx, const SlotVol &in, SlotVol &out, int *overflow);
+int slot_negate_inv(vo_ctx *ctx, const SlotVol &in, const vo_grid &g, SlotVol &out, int *overflow);
+int slot_max_count(vo_ctx *ctx, const SlotVol &v, int *d_max);
+int slot_to_volume(vo_ctx *ctx, const SlotVol &v, vo_volume **out);
+
+// Batched executor (vo_fast.cu).
+int morph_batched_fast(vo_ctx *ctx, int n, const int *ops, const double *radii, const vo_volume *const *ins,
+                       vo_volume **outs, vo_timings *tm);
+
 // Volume allocation (vo_api.cu).
 int volume_alloc(vo_ctx *ctx, const vo_grid &g, int64_t nseg, vo_volume **out);
 

@@ -732,6 +732,153 @@ __global__ void k_norm_big(const int32_t *__restrict__ offs, const double2 *__re
   }
 }
 
+// ---------------------------------------------------------------- slot layout
+
+// Fixed-capacity "slot" volumes hold column c's segments at z[c*cap ..
+// c*cap + n_c) with end[c] = c*cap + n_c; they let a chain of stages run
+// without knowing output sizes in advance (no host synchronisation), which is
+// what the batched executor needs to capture a whole batch in a CUDA graph.
+
+// negate_ray on the values v[0..n2) within [zmin, zmax] (MorphologyOperators.cpp:230-259);
+// returns the number of values written to out.
+__device__ int negate_vals(const double *v, int n2, double zmin, double zmax, double *out) {
+  if (n2 == 0) {
+    out[0] = zmin;
+    out[1] = zmax;
+    return 2;
+  }
+  int w = 0, k = 0;
+  if (v[0] == zmin)
+    k = 1;
+  else
+    out[w++] = zmin;
+  for (; k < n2; ++k) out[w++] = v[k];
+  if (out[w - 1] == zmax)
+    --w;
+  else
+    out[w++] = zmax;
+  return w;
+}
+
+// negate_ray_range (MorphologyOperators.cpp:282-315); returns the value count.
+__device__ int negate_range_vals(const double *v, int n2, double ymin, double ymax, double *out) {
+  if (n2 == 0) {
+    out[0] = ymin;
+    out[1] = ymax;
+    return 2;
+  }
+  int b = 0, e = n2, count_first = 0, count_last = 0, w = 0;
+  while (v[b] <= ymin) {
+    ++b;
+    ++count_first;
+    if (b == e) break;
+  }
+  int has_front = (count_first % 2 == 0);
+  for (;;) {
+    double back;
+    if (e > b)
+      back = v[e - 1];
+    else if (has_front)
+      back = ymin;
+    else
+      break;
+    if (!(back >= ymax)) break;
+    if (e > b)
+      --e;
+    else
+      has_front = 0;
+    ++count_last;
+    if (e == b && !has_front) break;
+  }
+  if (has_front) out[w++] = ymin;
+  for (int k = b; k < e; ++k) out[w++] = v[k];
+  if (count_last % 2 == 0) out[w++] = ymax;
+  return w;
+}
+
+__global__ void k_slot_beg(int ncols, int cap, int32_t *beg) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < ncols) beg[c] = c * cap;
+}
+
+__global__ void k_slot_end_from_counts(int ncols, int cap, const int32_t *counts, int32_t *end) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < ncols) end[c] = c * cap + counts[c];
+}
+
+// negate (Voronoi.cpp:18-55) into a grown (nx+2) x (ny+2) slot volume.
+__global__ void k_negate_slot(int nx, int ny, const int32_t *__restrict__ beg, const int32_t *__restrict__ end,
+                              const double2 *__restrict__ z, double zmin, double zmax, int cap, int32_t *oend,
+                              double2 *oz, int *overflow) {
+  const int NX = nx + 2, NY = ny + 2;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= NX * NY) return;
+  const int src = negate_src(i % NX, i / NX, nx, ny);
+  const int n2 = src >= 0 ? 2 * (end[src] - beg[src]) : 0;
+  if (n2 / 2 + 1 > cap) {
+    atomicOr(overflow, 1);
+    oend[i] = i * cap;
+    return;
+  }
+  const int w = negate_vals(src >= 0 ? (const double *)(z + beg[src]) : nullptr, n2, zmin, zmax,
+                            (double *)(oz + (size_t)i * cap));
+  oend[i] = i * cap + w / 2;
+}
+
+// Inverted-pair normalisation (see norm_column) slot to slot.
+__global__ void k_norm_slot(int ncols, const int32_t *__restrict__ beg, const int32_t *__restrict__ end,
+                            const double2 *__restrict__ z, int cap, int32_t *oend, double2 *oz, int *overflow) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncols) return;
+  double2 buf[kNormCap];
+  const int k0 = beg[c], k1 = end[c];
+  int n = -1;
+  if (k1 - k0 + 2 <= cap) n = norm_column(z, k0, k1, buf, kNormCap, oz + (size_t)c * cap);
+  if (n < 0 || n > cap) {
+    atomicOr(overflow, 1);
+    n = 0;
+  }
+  oend[c] = c * cap + n;
+}
+
+// negateInv (Voronoi.cpp:57-89): crop the one-column border, complement within [ymin, ymax].
+__global__ void k_negate_inv_slot(int nx, int ny, const int32_t *__restrict__ beg, const int32_t *__restrict__ end,
+                                  const double2 *__restrict__ z, double ymin, double ymax, int cap, int32_t *oend,
+                                  double2 *oz, int *overflow) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nx * ny) return;
+  const int c = (i % nx + 1) + (nx + 2) * (i / nx + 1);
+  const int n2 = 2 * (end[c] - beg[c]);
+  if (n2 / 2 + 1 > cap) {
+    atomicOr(overflow, 1);
+    oend[i] = i * cap;
+    return;
+  }
+  const int w = negate_range_vals((const double *)(z + beg[c]), n2, ymin, ymax, (double *)(oz + (size_t)i * cap));
+  oend[i] = i * cap + w / 2;
+}
+
+__global__ void k_slot_counts(int ncols, const int32_t *beg, const int32_t *end, int32_t *counts, int *maxc) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  int n = 0;
+  if (c < ncols) {
+    n = end[c] - beg[c];
+    if (counts) counts[c] = n;
+  }
+  if (maxc) {
+    for (int o = 16; o > 0; o >>= 1) n = max(n, __shfl_xor_sync(0xffffffffu, n, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(maxc, n);
+  }
+}
+
+__global__ void k_slot_compact(int ncols, const int32_t *__restrict__ beg, const double2 *__restrict__ z,
+                               const int32_t *__restrict__ ooffs, double2 *__restrict__ oz) {
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w >= ncols) return;
+  const int n = ooffs[w + 1] - ooffs[w];
+  for (int k = lane; k < n; k += 32) oz[ooffs[w] + k] = z[beg[w] + k];
+}
+
 }  // namespace
 
 // ================================================================ host side
@@ -1075,6 +1222,128 @@ int erode(vo_ctx *ctx, int method, double R, const vo_volume *in, vo_volume **ou
     return rc;
   }
   VO_CK(ctx, cudaGetLastError());
+  *out = res;
+  return VO_OK;
+}
+
+// ---------------------------------------------------------------- slot launchers
+
+namespace {
+inline int nblocks(int64_t n, int t) { return (int)((n + t - 1) / t); }
+}  // namespace
+
+int slot_alloc(vo_ctx *ctx, const vo_grid &g, int cap, SlotVol &v) {
+  v = SlotVol();
+  v.grid = g;
+  v.cap = cap;
+  const int ncols = g.nx * g.ny;
+  int rc = dalloc(ctx, &v.beg, (size_t)ncols);
+  if (!rc) rc = dalloc(ctx, &v.end, (size_t)ncols);
+  if (!rc) rc = dalloc(ctx, &v.z, (size_t)ncols * (size_t)std::max(cap, 1));
+  if (rc) {
+    slot_free(ctx, v);
+    return rc;
+  }
+  v.owns = true;
+  k_slot_beg<<<nblocks(ncols, 256), 256, 0, ctx->stream>>>(ncols, cap, v.beg);
+  ctx->launches += 1;
+  return VO_OK;
+}
+
+void slot_free(vo_ctx *ctx, SlotVol &v) {
+  if (v.owns) {
+    dfree(ctx, v.beg);
+    dfree(ctx, v.end);
+    dfree(ctx, v.z);
+  }
+  v = SlotVol();
+}
+
+SlotVol slot_view(const vo_volume *in, int cap) {
+  SlotVol v;
+  v.grid = in->grid;
+  v.cap = cap;
+  v.beg = in->offs;
+  v.end = in->offs + 1;
+  v.z = in->z;
+  v.owns = false;
+  return v;
+}
+
+void slot_end_from_counts(vo_ctx *ctx, SlotVol &v, const int32_t *counts) {
+  const int ncols = v.grid.nx * v.grid.ny;
+  k_slot_end_from_counts<<<nblocks(ncols, 256), 256, 0, ctx->stream>>>(ncols, v.cap, counts, v.end);
+  ctx->launches += 1;
+}
+
+int slot_negate(vo_ctx *ctx, const SlotVol &in, SlotVol &out, int *overflow) {
+  const vo_grid &g = in.grid;
+  const double zmin = g.origin[2] / g.spacing - 1;
+  const double zmax = g.origin[2] / g.spacing + 2 * g.padding + g.extent[2] / g.spacing + 1;
+  vo_grid g2 = g;
+  g2.nx += 2;
+  g2.ny += 2;
+  int rc = slot_alloc(ctx, g2, in.cap + 1, out);
+  if (rc) return rc;
+  k_negate_slot<<<nblocks((int64_t)g2.nx * g2.ny, 256), 256, 0, ctx->stream>>>(
+      g.nx, g.ny, in.beg, in.end, in.z, zmin, zmax, out.cap, out.end, out.z, overflow);
+  ctx->launches += 1;
+  return VO_OK;
+}
+
+int slot_normalize(vo_ctx *ctx, const SlotVol &in, SlotVol &out, int *overflow) {
+  int rc = slot_alloc(ctx, in.grid, in.cap + 2, out);
+  if (rc) return rc;
+  const int ncols = in.grid.nx * in.grid.ny;
+  k_norm_slot<<<nblocks(ncols, 128), 128, 0, ctx->stream>>>(ncols, in.beg, in.end, in.z, out.cap, out.end, out.z,
+                                                            overflow);
+  ctx->launches += 1;
+  return VO_OK;
+}
+
+int slot_negate_inv(vo_ctx *ctx, const SlotVol &in, const vo_grid &g, SlotVol &out, int *overflow) {
+  const double zmin = g.origin[2] / g.spacing - 1;
+  const double zmax = g.origin[2] / g.spacing + 2 * g.padding + g.extent[2] / g.spacing + 1;
+  int rc = slot_alloc(ctx, g, in.cap + 1, out);
+  if (rc) return rc;
+  k_negate_inv_slot<<<nblocks((int64_t)g.nx * g.ny, 256), 256, 0, ctx->stream>>>(
+      g.nx, g.ny, in.beg, in.end, in.z, zmin + 1, zmax - 1, out.cap, out.end, out.z, overflow);
+  ctx->launches += 1;
+  return VO_OK;
+}
+
+int slot_max_count(vo_ctx *ctx, const SlotVol &v, int *d_max) {
+  const int ncols = v.grid.nx * v.grid.ny;
+  k_slot_counts<<<nblocks(ncols, 256), 256, 0, ctx->stream>>>(ncols, v.beg, v.end, nullptr, d_max);
+  ctx->launches += 1;
+  return VO_OK;
+}
+
+int slot_to_volume(vo_ctx *ctx, const SlotVol &v, vo_volume **out) {
+  const int ncols = v.grid.nx * v.grid.ny;
+  int32_t *counts = nullptr;
+  int rc = dalloc(ctx, &counts, (size_t)ncols);
+  if (rc) return rc;
+  vo_volume *res = nullptr;
+  long long total = 0;
+  k_slot_counts<<<nblocks(ncols, 256), 256, 0, ctx->stream>>>(ncols, v.beg, v.end, counts, nullptr);
+  ctx->launches += 1;
+  rc = volume_alloc(ctx, v.grid, 0, &res);
+  if (!rc) rc = scan_counts(ctx, counts, res->offs, ncols, &total);
+  if (!rc) {
+    res->nseg = total;
+    rc = dalloc(ctx, &res->z, (size_t)total);
+  }
+  if (!rc) {
+    k_slot_compact<<<nblocks((int64_t)ncols * 32, 256), 256, 0, ctx->stream>>>(ncols, v.beg, v.z, res->offs,
+                                                                               res->z);
+    ctx->launches += 1;
+  }
+  dfree(ctx, counts);
+  if (rc) {
+    if (res) vo_volume_free(ctx, res);
+    return rc;
+  }
   *out = res;
   return VO_OK;
 }
