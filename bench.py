@@ -7,9 +7,16 @@ configuration the headline metric is quoted on. The input (~345 MB of FP64
 pairs) is larger than L2 (129 MB), so no flush is needed between steps.
 
   value : Mcolumns/s with the input resident in HBM (device-timed, CUDA events
-          on the library's stream), whole job = all ranks.
+          on the library's stream), whole job = all ranks. The default method
+          is the batch plan (vo_batch_*) with the learned sizer: one step is a
+          replay of the captured graph plus the conversion of the output slots
+          to CSR. The plan is built once before the warm-up.
+  arms  : the plain GPU method (FP64 separable, count then fill) and the
+          single-volume FP32-guarded method on the same volume, for the
+          "plain vs batched+learned" comparison.
   e2e   : the same metric through the C ABI from pinned host buffers: upload,
-          dilation and download of the result inside the timed region.
+          vo_morph_batched (plan, replay, outputs) and download of the result
+          inside the timed region.
   cpu_baseline : the reference's own `ours` (oracle/_ref, multithreaded) or,
           where the reference could not be built, the oracle restatement, timed
           on a bounded slab of the same workload (rank 0, N=1).
@@ -44,7 +51,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--method", default="fast", choices=["separable", "brute", "fast"])
+    ap.add_argument("--method", default="batched", choices=["batched", "separable", "brute", "fast"],
+                    help="batched: a captured batch plan with the learned sizer (the headline)")
+    ap.add_argument("--no-sizer", action="store_true", help="batched plan without the learned sizer")
+    ap.add_argument("--no-arms", action="store_true", help="skip the plain / single-volume comparison arms")
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--radius", type=float, default=RADIUS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -237,37 +247,80 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
-    # ---------------- device-resident arm (value)
+    # ---------------- learned sizer (batched arms)
+    sizer = None
+    if args.method == "batched" and not args.no_sizer:
+        from voroffset_gb300.train_sizer import WEIGHTS, load
+        if os.path.exists(WEIGHTS):
+            sizer = load(ctx)
+            ctx.set_sizer(sizer)
+
     vin = ctx.upload(grid, offs, z)
     ctx.sync()
-    for _ in range(args.warmup):
-        out, t = ctx.morph(vin, "dilation", args.radius, args.method)
-        out.free()
+
+    def timed(step, steps, warmup):
+        """Device time (CUDA events on the library stream) of `steps` calls of step()."""
+        for _ in range(warmup):
+            step()
+        barrier()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(steps):
+            step()
+        ev1.record(stream)
+        barrier()
+        return maxreduce(ev0.elapsed_time(ev1))
+
+    acc = {"launches": 0, "kernel_ms": 0.0, "out_segs": 0, "mid": 0}
+
+    def single_step(method):
+        def f():
+            out, t = ctx.morph(vin, "dilation", args.radius, method)
+            acc["launches"] += t["kernel_launches"]
+            acc["kernel_ms"] += max(t["kernel_ms"])
+            acc["out_segs"] = out.nseg
+            acc["mid"] = t["mid_pieces"]
+            out.free()
+        return f
+
+    plan = None
+    plan_stats = None
+    if args.method == "batched":
+        plan = ctx.batch([vin], ["dilation"], [args.radius], "fast")
+        plan_stats = plan.stats()
+
+        def step():
+            t = plan.run()
+            outs = plan.outputs()
+            acc["launches"] += t["kernel_launches"] + 5  # graph kernels + slot -> CSR (counts, 3 scan, compact)
+            acc["kernel_ms"] += t["pass2_ms"]
+            acc["out_segs"] = outs[0].nseg
+            outs[0].free()
+    else:
+        step = single_step(args.method)
+
+    # ---------------- device-resident arm (value)
     clocks = ClockSampler(local)
     clocks.start()
-    barrier()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
-    launches = 0
-    kms = np.zeros(4)
-    tims = []
-    out_segs = 0
-    mid = 0
-    for _ in range(args.steps):
-        out, t = ctx.morph(vin, "dilation", args.radius, args.method)
-        launches += t["kernel_launches"]
-        kms += np.array(t["kernel_ms"])
-        tims.append(t)
-        out_segs = out.nseg
-        mid = t["mid_pieces"]
-        out.free()
-    ev1.record(stream)
-    barrier()
+    dev_ms = timed(step, args.steps, args.warmup)
     clk = clocks.stop()
-    dev_ms = ev0.elapsed_time(ev1)
-    dev_ms = maxreduce(dev_ms)
+    launches, kernel_total_ms, out_segs, mid = acc["launches"], acc["kernel_ms"], acc["out_segs"], acc["mid"]
     value = world * ncols * args.steps / (dev_ms / 1e3) / 1e6
+    # kernel time of the warm-up steps was accumulated too: keep the timed steps only
+    kernel_ms = kernel_total_ms * args.steps / (args.steps + args.warmup)
+    launches = launches * args.steps // (args.steps + args.warmup)
+
+    # ---------------- comparison arms on the same volume: the plain GPU method
+    # (FP64 separable, count then fill) and the single-volume FP32-guarded method
+    arms = {}
+    if args.method == "batched" and not args.no_arms:
+        for name, method, k in (("plain_separable_fp64", "separable", max(1, args.steps // 2)),
+                                ("fast_single_volume", "fast", args.steps)):
+            ms = timed(single_step(method), k, 1)
+            arms[name] = {"value": world * ncols * k / (ms / 1e3) / 1e6, "unit": "Mcolumns/s",
+                          "ms_per_step": ms / k, "steps": k}
+        arms["batched_vs_plain"] = value / arms["plain_separable_fp64"]["value"]
 
     # ---------------- end-to-end arm (pinned host buffers through the C ABI)
     pin_offs = torch.empty(offs.size, dtype=torch.int32, pin_memory=True).numpy()
@@ -276,53 +329,58 @@ def main():
     pin_z[:z.size] = z
     out_offs = torch.empty(ncols + 1, dtype=torch.int32, pin_memory=True).numpy()
     out_z = torch.empty(max(2 * out_segs, 2), dtype=torch.float64, pin_memory=True).numpy()
-    for _ in range(max(1, args.warmup)):
+
+    def e2e_step():
         v = ctx.upload(grid, pin_offs, pin_z[:z.size])
-        o, _ = ctx.morph(v, "dilation", args.radius, args.method)
-        ctx.download_into(o, out_offs, out_z)
+        if args.method == "batched":
+            outs, _ = ctx.morph_batched([v], ["dilation"], [args.radius], "fast")
+            o = outs[0]
+        else:
+            o, _ = ctx.morph(v, "dilation", args.radius, args.method)
+        n_o, n_z = ctx.download_into(o, out_offs, out_z)
         o.free()
         v.free()
+        return 4 * n_o + 8 * n_z
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
     barrier()
     t0 = time.perf_counter()
     d2h = 0
     for _ in range(args.steps):
-        v = ctx.upload(grid, pin_offs, pin_z[:z.size])
-        o, _ = ctx.morph(v, "dilation", args.radius, args.method)
-        n_o, n_z = ctx.download_into(o, out_offs, out_z)
-        d2h = 4 * n_o + 8 * n_z
-        o.free()
-        v.free()
+        d2h = e2e_step()
     barrier()
     e2e_s = maxreduce(time.perf_counter() - t0)
     e2e = world * ncols * args.steps / e2e_s / 1e6
 
     # ---------------- roofline of the dominant kernel
-    names = ["pass1_count", "pass1_fill", "pass2_count", "pass2_fill"]
-    per_launch = kms / args.steps
-    dom = int(np.argmax(per_launch))
+    kname = {"batched": "k_fast_batched", "fast": "k_fast", "separable": "k_pass2", "brute": "k_brute"}[args.method]
+    per_launch = kernel_ms / args.steps
     alg_bytes = 4 * (ncols + 1) + 16 * int(offs[-1]) + 4 * (ncols + 1) + 16 * int(out_segs)
     peak, peak_kind = peaks()
-    achieved = alg_bytes / (per_launch[dom] / 1e3) / 1e9 if per_launch[dom] > 0 else 0.0
-    tpc = traffic_per_column(names[dom], args.radius)
+    achieved = alg_bytes / (per_launch / 1e3) / 1e9 if per_launch > 0 else 0.0
+    tpc = traffic_per_column(kname, args.radius)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": None if tpc is None else tpc * ncols,
-                "kernel": names[dom], "kernel_ms": per_launch[dom], "peak_source": peak_kind,
+                "kernel": kname, "kernel_ms": per_launch, "peak_source": peak_kind,
                 "algorithmic_bytes": alg_bytes,
                 "op_achieved": alg_bytes / (dev_ms / args.steps / 1e3) / 1e9}
 
+    dtype = "f64" if args.method in ("separable", "brute") else "f32+f64"
+    cfg = {"workload": f"{args.workload} dilation r={args.radius:g}", "grid": [grid.nx, grid.ny],
+           "method": args.method if args.method != "batched" else "batched+learned" if sizer else "batched",
+           "in_segments": int(offs[-1]), "out_segments": int(out_segs), "mid_pieces": int(mid),
+           "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas" if world > 1 else "single GPU"}
+    if plan_stats is not None:
+        cfg["plan"] = {k: plan_stats[k] for k in ("slot_bytes", "tiles", "tile_rows", "graph_nodes",
+                                                  "graph_kernels", "learned", "plan_ms", "tune_ms")}
     line = {"metric": METRIC, "value": value, "unit": "Mcolumns/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.method != "fast" else "f32+f64",
-            "data": "synthetic",
-            "config": {"workload": f"{args.workload} dilation r={args.radius:g}", "grid": [grid.nx, grid.ny],
-                       "method": args.method, "in_segments": int(offs[-1]), "out_segments": int(out_segs),
-                       "mid_pieces": int(mid), "l2": "inputs larger than L2 (no flush)",
-                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic", "config": cfg,
             "e2e": {"value": e2e, "unit": "Mcolumns/s", "h2d_bytes_per_step": int(in_bytes),
                     "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(launches),
-            "kernel_ms_per_step": {n: float(x) for n, x in zip(names, per_launch)},
-            "roofline": roofline, "clocks": clk,
+            "roofline": roofline, "clocks": clk, "arms": arms,
             "gsegments_per_s": world * (int(offs[-1]) + int(out_segs)) * args.steps / (dev_ms / 1e3) / 1e9}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
@@ -330,6 +388,11 @@ def main():
                                                                args.cpu_seconds).items() if k != "rows"}
         except Exception as exc:  # the baseline is reported, never required
             line["cpu_baseline"] = {"value": None, "error": str(exc)}
+    if plan is not None:
+        plan.free()
+    if sizer is not None:
+        ctx.set_sizer(None)
+        sizer.free()
     vin.free()
     ctx.close()
     if rank == 0:

@@ -120,6 +120,35 @@ int vo_morph(vo_ctx *ctx, int op, int method, double radius, const vo_volume *in
 int vo_morph_batched(vo_ctx *ctx, int n, const int *ops, const double *radii, int method,
                      const vo_volume *const *ins, vo_volume **outs, vo_timings *timings);
 
+/* Batch plans (no reference counterpart): the work of vo_morph_batched with
+ * VO_METHOD_FAST, split so that the planned work can be replayed. Create
+ * plans the chains of every volume (erosion -> dilation for opening and
+ * closing), sizes the output slots (from the attached sizer, see
+ * vo_set_sizer, or a fixed capacity), orders the persistent work queue,
+ * chooses the block shape with the autotuner (cached per context), and
+ * captures all device steps into one CUDA graph; it keeps pointers to `ins`,
+ * which must outlive the plan and keep their contents. Run replays the graph
+ * and re-runs, one by one through vo_morph's path, the volumes whose output
+ * overflowed its slots. Outputs returns new CSR volumes (caller frees). */
+typedef struct vo_batch vo_batch;
+typedef struct {
+  int64_t slot_bytes;   /* output slot memory of the dilations */
+  int32_t tiles;        /* work-queue items over all rounds */
+  int32_t tile_rows;    /* rows of 32 columns per block chosen by the autotuner (last round) */
+  int32_t graph_nodes;  /* nodes of the captured graph */
+  int32_t graph_kernels;/* kernel launches per replay */
+  int32_t learned;      /* 1 when slots and queue came from a sizer */
+  int32_t reruns;       /* volumes re-run by the last vo_batch_run */
+  double plan_ms;       /* host time of vo_batch_create */
+  double tune_ms[4];    /* autotuner sample times for 1, 2, 4, 8 rows (0: cached / not run) */
+} vo_batch_stats;
+int vo_batch_create(vo_ctx *ctx, int n, const int *ops, const double *radii, int method,
+                    const vo_volume *const *ins, vo_batch **out);
+int vo_batch_run(vo_ctx *ctx, vo_batch *b, vo_timings *timings);
+int vo_batch_outputs(vo_ctx *ctx, vo_batch *b, vo_volume **outs);
+int vo_batch_stats_get(vo_ctx *ctx, const vo_batch *b, vo_batch_stats *stats);
+void vo_batch_destroy(vo_ctx *ctx, vo_batch *b);
+
 /* Mesh -> dexels by vertical ray casting (replaces create_dexels + compute_sign,
  * Dexelize.cpp:166-274). verts[3*nv] FP64, tris[3*nt] int32 (0-based).
  * num_dexels > 0: spacing = longest bbox side / num_dexels; otherwise *spacing
@@ -147,6 +176,49 @@ int vo_xor_volume(vo_ctx *ctx, const vo_volume *a, const vo_volume *b, double *v
  * or threads) race and must be serialised by the caller. */
 int vo_xor_volume_noalloc(const vo_grid *grid, const int32_t *offs_a, const double *z_a,
                           const int32_t *offs_b, const double *z_b, void *stream, double *volume);
+
+/* ---- learned sizing for vo_morph_batched (no reference counterpart) ----
+ * A small MLP (16 tile features -> 64 -> 64 -> 3 outputs, ReLU, BF16 weights
+ * with FP32 accumulation) predicts per 32 x 32 tile of output columns
+ * log2(1 + max output segments per column), log2(1 + mean output segments)
+ * and log2(1 + candidate intervals per column). When a sizer is attached to a
+ * context, vo_morph_batched with VO_METHOD_FAST sizes each tile's output slots
+ * from the first prediction and orders its work queue by the third; a column
+ * that outgrows its slot is detected exactly and its volume re-runs through
+ * vo_morph, so results never depend on the network. Training runs on the
+ * device (mean squared error, Adam) with hand-written forward / backward
+ * kernels. */
+#define VO_SIZER_FEATURES 16
+#define VO_SIZER_OUTPUTS 3
+typedef struct vo_sizer vo_sizer;
+/* New network with He-uniform weights drawn from `seed`. */
+int vo_sizer_create(vo_ctx *ctx, uint64_t seed, vo_sizer **out);
+void vo_sizer_destroy(vo_ctx *ctx, vo_sizer *s);
+/* Number of FP32 parameters (W1[16][64], b1, W2[64][64], b2, W3[64][4], b3). */
+int vo_sizer_num_params(void);
+/* Copy parameters in (resets the optimiser state) / out. count must equal
+ * vo_sizer_num_params(). */
+int vo_sizer_set_params(vo_ctx *ctx, vo_sizer *s, const float *params, int count);
+int vo_sizer_get_params(vo_ctx *ctx, const vo_sizer *s, float *params, int count);
+/* Features [ntiles][VO_SIZER_FEATURES] of a volume's tiles for a dilation of
+ * `radius`; feats == NULL returns the tile count only. */
+int vo_sizer_tile_features(vo_ctx *ctx, const vo_volume *v, double radius, float *feats, int *ntiles);
+/* Training targets [ntiles][VO_SIZER_OUTPUTS] from an input and its dilation. */
+int vo_sizer_tile_targets(vo_ctx *ctx, const vo_volume *in, const vo_volume *result, double radius,
+                          float *targets, int *ntiles);
+/* Predictions [n][VO_SIZER_OUTPUTS] for host features [n][VO_SIZER_FEATURES]. */
+int vo_sizer_forward(vo_ctx *ctx, const vo_sizer *s, const float *feats, int n, float *pred);
+/* Gradient of the mean squared error over the n samples w.r.t. every
+ * parameter (grads[vo_sizer_num_params()]) and the loss, without updating. */
+int vo_sizer_gradients(vo_ctx *ctx, vo_sizer *s, const float *feats, const float *targets, int n,
+                       float *grads, float *loss);
+/* `steps` full-batch Adam steps at learning rate lr; *final_loss (may be NULL)
+ * is the loss after the last step. */
+int vo_sizer_train(vo_ctx *ctx, vo_sizer *s, const float *feats, const float *targets, int n, int steps,
+                   float lr, float *final_loss);
+/* Attach (s != NULL) or detach (NULL) a sizer used by vo_morph_batched. The
+ * context does not own it. */
+int vo_set_sizer(vo_ctx *ctx, vo_sizer *s);
 
 /* ---- host utilities (no device work) ---- */
 

@@ -50,8 +50,8 @@ def test_batched_equals_single_calls(ctx, vo):
 
 
 def test_batched_overflow_reruns(ctx, vo, oracle):
-    # 60 thin plates per column: more union intervals than a slot holds
-    nx, ny, k = 24, 20, 60
+    # 150 thin plates per column: more union intervals than the second tier holds
+    nx, ny, k = 24, 20, 150
     base = np.arange(k, dtype=np.float64) * 3.0
     z = np.tile(np.stack([base, base + 1.0], 1).reshape(-1), nx * ny)
     offs = (np.arange(nx * ny + 1) * k).astype(np.int32)
@@ -62,3 +62,51 @@ def test_batched_overflow_reruns(ctx, vo, oracle):
     assert t["overflow_columns"] >= 1  # the first volume re-ran through the single-volume path
     assert_same(ctx.download(outs[0]), oracle.morph(ogrid(oracle, g), offs, z, 0.9, "dilation"), tol=0.0)
     assert_same(ctx.download(outs[1]), oracle.morph(ogrid(oracle, g2), o2, z2, 3.0, "closing"), tol=0.0)
+
+
+def test_plan_replays_identically(ctx, vo):
+    items = _batch(vo, 8, 21)
+    vols = [ctx.upload(g, o, z) for g, o, z, _, _ in items]
+    b = ctx.batch(vols, [it[4] for it in items], [it[3] for it in items])
+    st = b.stats()
+    assert st["graph_nodes"] > 0 and st["graph_kernels"] > 0
+    assert st["tile_rows"] in (1, 2, 4, 8)
+    b.run()
+    first = [ctx.download(o) for o in b.outputs()]
+    t = b.run()
+    assert t["pass2_ms"] > 0
+    second = [ctx.download(o) for o in b.outputs()]
+    for a, c in zip(first, second):
+        assert np.array_equal(a[0], c[0]) and np.array_equal(a[1], c[1])
+    # a second plan of the same shape reuses the autotuner's choice
+    b2 = ctx.batch(vols, [it[4] for it in items], [it[3] for it in items])
+    assert b2.stats()["tune_ms"] == [0.0, 0.0, 0.0, 0.0]
+    assert b2.stats()["tile_rows"] == st["tile_rows"]
+
+
+def test_plan_rejects_other_methods(ctx, vo):
+    g, o, z = vo.synth_volume(vo.SynthSpec(32, n_spheres=4, s_rmin=2, s_rmax=6, seed=1))
+    v = ctx.upload(g, o, z)
+    with pytest.raises(vo.GpuError):
+        ctx.batch([v], ["dilation"], [2.0], method="separable")
+
+
+def test_batched_second_tier_without_rerun(ctx, vo, oracle):
+    """A few columns with 40-interval unions: the second tier computes them and
+    the spill region takes them, so no volume re-runs."""
+    nx, ny, k = 64, 48, 40
+    g0, o0, z0 = vo.synth_volume(vo.SynthSpec(64, n_spheres=30, s_rmin=2, s_rmax=8, seed=8, ny=48, zmax=200))
+    cols = [z0[2 * o0[c]:2 * o0[c + 1]] for c in range(nx * ny)]
+    base = 300.0 + np.arange(k) * 3.0
+    plates = np.stack([base, base + 1.0], 1).reshape(-1)
+    for y in range(10, 13):
+        for x in range(20, 24):
+            cols[x + nx * y] = np.concatenate([cols[x + nx * y], plates])
+    offs = np.zeros(nx * ny + 1, np.int32)
+    offs[1:] = np.cumsum([c.size // 2 for c in cols])
+    z = np.concatenate(cols)
+    g = vo.Grid(nx, ny, (0, 0, 0), (nx, ny, 500), 1.0, 0)
+    v = ctx.upload(g, offs, z)
+    outs, t = ctx.morph_batched([v], ["dilation"], [0.9], "fast")
+    assert t["overflow_columns"] == 0
+    assert_same(ctx.download(outs[0]), oracle.morph(ogrid(oracle, g), offs, z, 0.9, "dilation"), tol=0.0)

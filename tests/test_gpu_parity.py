@@ -134,10 +134,12 @@ def test_gpu_zero_length_and_touching_segments(ctx, vo, oracle, method):
 
 
 @pytest.mark.parametrize("method", METHODS)
-def test_gpu_overflow_path(ctx, vo, oracle, method):
+@pytest.mark.parametrize("k", [60, 150])
+def test_gpu_overflow_path(ctx, vo, oracle, method, k):
     # many thin disjoint plates per column overflow the fast kernels' working
-    # lists; the large-capacity re-run must give the same answer
-    nx, ny, k = 40, 40, 60
+    # lists (60: the 128-interval second tier of the FP32 method; 150: its
+    # FP64 list); the large-capacity re-runs must give the same answer
+    nx, ny = 40, 40
     base = np.arange(k, dtype=np.float64) * 3.0
     z = np.stack([base, base + 1.0], 1).reshape(-1)
     offs = (np.arange(nx * ny + 1) * k).astype(np.int32)

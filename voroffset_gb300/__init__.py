@@ -51,6 +51,16 @@ class _SynthParams(C.Structure):
                 ("c_rmin", C.c_double), ("c_rmax", C.c_double), ("seed", C.c_uint64)]
 
 
+class _BatchStats(C.Structure):
+    _fields_ = [("slot_bytes", C.c_int64), ("tiles", C.c_int32), ("tile_rows", C.c_int32),
+                ("graph_nodes", C.c_int32), ("graph_kernels", C.c_int32), ("learned", C.c_int32),
+                ("reruns", C.c_int32), ("plan_ms", C.c_double), ("tune_ms", C.c_double * 4)]
+
+
+SIZER_FEATURES = 16
+SIZER_OUTPUTS = 3
+
+
 @dataclass
 class Grid:
     """CompressedVolume geometry (CompressedVolumeBase.h:17-21); origin already padded."""
@@ -102,6 +112,25 @@ SIGNATURES = {
                               C.POINTER(C.c_double), C.c_int, C.c_int, C.POINTER(_P)]),
     "vo_xor_volume": (C.c_int, [_P, _P, _P, C.POINTER(C.c_double)]),
     "vo_xor_volume_noalloc": (C.c_int, [C.POINTER(_Grid), _P, _P, _P, _P, _P, C.POINTER(C.c_double)]),
+    "vo_batch_create": (C.c_int, [_P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_int,
+                                  C.POINTER(_P), C.POINTER(_P)]),
+    "vo_batch_run": (C.c_int, [_P, _P, C.POINTER(_Timings)]),
+    "vo_batch_outputs": (C.c_int, [_P, _P, C.POINTER(_P)]),
+    "vo_batch_stats_get": (C.c_int, [_P, _P, C.POINTER(_BatchStats)]),
+    "vo_batch_destroy": (None, [_P, _P]),
+    "vo_sizer_create": (C.c_int, [_P, C.c_uint64, C.POINTER(_P)]),
+    "vo_sizer_destroy": (None, [_P, _P]),
+    "vo_sizer_num_params": (C.c_int, []),
+    "vo_sizer_set_params": (C.c_int, [_P, _P, C.POINTER(C.c_float), C.c_int]),
+    "vo_sizer_get_params": (C.c_int, [_P, _P, C.POINTER(C.c_float), C.c_int]),
+    "vo_sizer_tile_features": (C.c_int, [_P, _P, C.c_double, C.POINTER(C.c_float), C.POINTER(C.c_int)]),
+    "vo_sizer_tile_targets": (C.c_int, [_P, _P, _P, C.c_double, C.POINTER(C.c_float), C.POINTER(C.c_int)]),
+    "vo_sizer_forward": (C.c_int, [_P, _P, C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_float)]),
+    "vo_sizer_gradients": (C.c_int, [_P, _P, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int,
+                                     C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "vo_sizer_train": (C.c_int, [_P, _P, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int, C.c_int,
+                                 C.c_float, C.POINTER(C.c_float)]),
+    "vo_set_sizer": (C.c_int, [_P, _P]),
     "vo_synth_volume": (C.c_int, [C.POINTER(_SynthParams), C.POINTER(C.c_int32),
                                   C.POINTER(C.POINTER(C.c_double)), C.POINTER(C.c_int64)]),
     "vo_synth_torus": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_uint64,
@@ -249,6 +278,25 @@ class Context:
                                            C.byref(t)), "vo_morph_batched")
         return [Volume(self, outs[i]) for i in range(n)], timings_dict(t)
 
+    def batch(self, vols, ops, radii, method: str = "fast") -> "Batch":
+        """A batch plan (vo_batch_create): planned, sized, tuned and captured once, replayed by run()."""
+        n = len(vols)
+        ops_a = (C.c_int * n)(*[OPS[o] for o in ops])
+        rad_a = (C.c_double * n)(*[float(r) for r in radii])
+        ins = (C.c_void_p * n)(*[v.handle for v in vols])
+        out = C.c_void_p()
+        self._check(lib().vo_batch_create(self.handle, n, ops_a, rad_a, METHODS[method], ins, C.byref(out)),
+                    "vo_batch_create")
+        return Batch(self, out.value, list(vols))
+
+    def sizer(self, seed: int = 1) -> "Sizer":
+        out = C.c_void_p()
+        self._check(lib().vo_sizer_create(self.handle, int(seed), C.byref(out)), "vo_sizer_create")
+        return Sizer(self, out.value)
+
+    def set_sizer(self, s: "Sizer | None"):
+        self._check(lib().vo_set_sizer(self.handle, s.handle if s is not None else None), "vo_set_sizer")
+
     def dexelize(self, verts, tris, num_dexels: int = 256, padding: int = 0, spacing: float = 1.0):
         verts = np.ascontiguousarray(verts, dtype=np.float64).reshape(-1)
         tris = np.ascontiguousarray(tris, dtype=np.int32).reshape(-1)
@@ -263,6 +311,114 @@ class Context:
         r = C.c_double()
         self._check(lib().vo_xor_volume(self.handle, a.handle, b.handle, C.byref(r)), "vo_xor_volume")
         return float(r.value)
+
+
+class Batch:
+    """A captured batch plan; keeps its input volumes alive."""
+
+    def __init__(self, ctx: Context, handle: int, inputs):
+        self.ctx, self.handle, self._inputs = ctx, handle, inputs
+
+    def run(self) -> dict:
+        t = _Timings()
+        self.ctx._check(lib().vo_batch_run(self.ctx.handle, self.handle, C.byref(t)), "vo_batch_run")
+        return timings_dict(t)
+
+    def outputs(self):
+        n = len(self._inputs)
+        outs = (C.c_void_p * max(n, 1))()
+        self.ctx._check(lib().vo_batch_outputs(self.ctx.handle, self.handle, outs), "vo_batch_outputs")
+        return [Volume(self.ctx, outs[i]) for i in range(n)]
+
+    def stats(self) -> dict:
+        s = _BatchStats()
+        self.ctx._check(lib().vo_batch_stats_get(self.ctx.handle, self.handle, C.byref(s)), "vo_batch_stats_get")
+        d = {k: getattr(s, k) for k, _ in _BatchStats._fields_}
+        d["tune_ms"] = list(s.tune_ms)
+        return d
+
+    def free(self):
+        if self.handle:
+            lib().vo_batch_destroy(self.ctx.handle, self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def _f32p(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class Sizer:
+    """The learned tile sizer (vo_sizer_*): an MLP trained and evaluated on the device."""
+
+    def __init__(self, ctx: Context, handle: int):
+        self.ctx, self.handle = ctx, handle
+
+    @staticmethod
+    def num_params() -> int:
+        return int(lib().vo_sizer_num_params())
+
+    def params(self) -> np.ndarray:
+        p = np.zeros(self.num_params(), np.float32)
+        self.ctx._check(lib().vo_sizer_get_params(self.ctx.handle, self.handle, _f32p(p), p.size),
+                        "vo_sizer_get_params")
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        self.ctx._check(lib().vo_sizer_set_params(self.ctx.handle, self.handle, _f32p(p), p.size),
+                        "vo_sizer_set_params")
+
+    def features(self, v: Volume, radius: float) -> np.ndarray:
+        n = C.c_int()
+        self.ctx._check(lib().vo_sizer_tile_features(self.ctx.handle, v.handle, float(radius), None, C.byref(n)),
+                        "vo_sizer_tile_features")
+        f = np.zeros((n.value, SIZER_FEATURES), np.float32)
+        self.ctx._check(lib().vo_sizer_tile_features(self.ctx.handle, v.handle, float(radius), _f32p(f),
+                                                     C.byref(n)), "vo_sizer_tile_features")
+        return f
+
+    def targets(self, v: Volume, result: Volume, radius: float) -> np.ndarray:
+        g = C.c_int()
+        nt = len(self.features(v, radius))
+        t = np.zeros((nt, SIZER_OUTPUTS), np.float32)
+        self.ctx._check(lib().vo_sizer_tile_targets(self.ctx.handle, v.handle, result.handle, float(radius),
+                                                    _f32p(t), C.byref(g)), "vo_sizer_tile_targets")
+        return t
+
+    def forward(self, feats) -> np.ndarray:
+        feats = np.ascontiguousarray(feats, dtype=np.float32)
+        out = np.zeros((len(feats), SIZER_OUTPUTS), np.float32)
+        self.ctx._check(lib().vo_sizer_forward(self.ctx.handle, self.handle, _f32p(feats), len(feats),
+                                               _f32p(out)), "vo_sizer_forward")
+        return out
+
+    def gradients(self, feats, targets):
+        feats = np.ascontiguousarray(feats, dtype=np.float32)
+        targets = np.ascontiguousarray(targets, dtype=np.float32)
+        g = np.zeros(self.num_params(), np.float32)
+        loss = C.c_float()
+        self.ctx._check(lib().vo_sizer_gradients(self.ctx.handle, self.handle, _f32p(feats), _f32p(targets),
+                                                 len(feats), _f32p(g), C.byref(loss)), "vo_sizer_gradients")
+        return g, float(loss.value)
+
+    def train(self, feats, targets, steps: int = 500, lr: float = 3e-3) -> float:
+        feats = np.ascontiguousarray(feats, dtype=np.float32)
+        targets = np.ascontiguousarray(targets, dtype=np.float32)
+        loss = C.c_float()
+        self.ctx._check(lib().vo_sizer_train(self.ctx.handle, self.handle, _f32p(feats), _f32p(targets),
+                                             len(feats), int(steps), float(lr), C.byref(loss)), "vo_sizer_train")
+        return float(loss.value)
+
+    def free(self):
+        if self.handle:
+            lib().vo_sizer_destroy(self.ctx.handle, self.handle)
+            self.handle = None
 
 
 def timings_dict(t: _Timings) -> dict:

@@ -98,6 +98,7 @@ int get_tables(vo_ctx *ctx, double R, int kmax, const DeviceTables **out) {
   if (e == cudaSuccess) e = cudaMalloc(&d->Hf, sizeof(float) * h.Hf.size());
   if (e == cudaSuccess) e = cudaMalloc(&d->Dx, sizeof(int) * h.Dx.size());
   if (e == cudaSuccess) e = cudaMalloc(&d->HB, sizeof(double) * h.HB.size());
+  if (e == cudaSuccess) e = cudaMalloc(&d->dH, sizeof(float) * 2 * h.H.size());
   if (e == cudaSuccess)
     e = cudaMemcpy(d->H, h.H.data(), sizeof(double) * h.H.size(), cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
@@ -106,11 +107,16 @@ int get_tables(vo_ctx *ctx, double R, int kmax, const DeviceTables **out) {
     e = cudaMemcpy(d->Dx, h.Dx.data(), sizeof(int) * h.Dx.size(), cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
     e = cudaMemcpy(d->HB, h.HB.data(), sizeof(double) * h.HB.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    launch_dh_tables(ctx->stream, h.Dy, h.W, d->H, d->Dx, d->dH);
+    e = cudaStreamSynchronize(ctx->stream);
+  }
   if (e != cudaSuccess) {
     cudaFree(d->H);
     cudaFree(d->Hf);
     cudaFree(d->Dx);
     cudaFree(d->HB);
+    cudaFree(d->dH);
     delete d;
     return cuda_error(ctx, e, "table upload");
   }
@@ -120,6 +126,7 @@ int get_tables(vo_ctx *ctx, double R, int kmax, const DeviceTables **out) {
     cudaFree(old->Hf);
     cudaFree(old->Dx);
     cudaFree(old->HB);
+    cudaFree(old->dH);
     delete old;
     ctx->tables.erase(ctx->tables.begin());
   }
@@ -206,6 +213,7 @@ void vo_destroy(vo_ctx *ctx) {
     cudaFree(d->Hf);
     cudaFree(d->Dx);
     cudaFree(d->HB);
+    cudaFree(d->dH);
     delete d;
   }
   for (auto &e : ctx->ev)

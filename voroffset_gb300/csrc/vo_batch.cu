@@ -1,0 +1,683 @@
+// Batch plans: many volumes of uneven grids, radii and operations (including
+// the erosion -> dilation chains of opening and closing) executed as one
+// CUDA graph, with every dilation of a round in one persistent launch
+// (VO_METHOD_FAST only; no reference counterpart beyond calling
+// VoronoiMorpho::dilation / erosion once per volume, Voronoi.h:18-29, and the
+// chaining of offset3d.cpp:124-133).
+//
+// Planning (vo_batch_create) walks the operation chains round by round. Every
+// device step is recorded as a launch closure; the plan runs the closures
+// eagerly only when a later step needs the data (the input features of a
+// learned-sized dilation, the capacity of a complement of a dilation result).
+// Per dilation:
+//   * output slots: with a sizer attached, every 32 x 32 tile of output
+//     columns gets the capacity the network predicts for its largest union
+//     (plus a margin, at most kUnionCapMid); without one, every column gets
+//     kUnionCap slots; either way a spill region takes the columns that need
+//     more (unions beyond kUnionCap are computed by the second-tier kernel);
+//   * work queue: (dilation, tile) items in decreasing predicted work (the
+//     network's per-tile candidate count, or the dilation's mean cost);
+//   * block shape: rows of 32 columns per block, chosen by the autotuner below
+//     and cached per context.
+// Then the closures are captured into one graph. vo_batch_run replays it and
+// re-runs, through the single-volume path, every volume whose overflow flag
+// is set (a union larger than its slot with the spill region exhausted, or
+// larger than kUnionCapMid), so results never depend on the predictions.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <functional>
+#include <vector>
+
+#include "vo_internal.cuh"
+
+using namespace vo;
+
+namespace {
+
+enum StepKind { kDil, kNeg, kNorm, kNegInv };
+
+// Operation chains (Voronoi.cpp:8-17 erosion; offset3d.cpp:124-133 opening/closing).
+std::vector<StepKind> steps_of(int op) {
+  switch (op) {
+    case VO_DILATION:
+      return {kDil};
+    case VO_EROSION:
+      return {kNeg, kNorm, kDil, kNegInv};
+    case VO_OPENING:
+      return {kNeg, kNorm, kDil, kNegInv, kDil};
+    default:
+      return {kDil, kNeg, kNorm, kDil, kNegInv};
+  }
+}
+
+using Launch = std::function<void(cudaStream_t)>;
+
+struct DilPlan {
+  int vol = 0;
+  SlotVol in, out;
+  const DeviceTables *T = nullptr;
+  float *zf = nullptr, *E = nullptr, *dom = nullptr;
+  float4 *segdom = nullptr;
+  unsigned int *maxbits = nullptr;
+  int2 *pairs = nullptr;
+  int *mid_list = nullptr, *mid_count = nullptr;
+  int npairs = 0;
+  int32_t *tcap = nullptr, *toff = nullptr;
+  int tiles32_x = 0, tiles32 = 0;
+  std::vector<float> tile_work;  // predicted candidates per column of each sizing tile
+  int spill_base = 0, spill_cap = 0;
+  int *spill_used = nullptr;
+  double cost = 0;  // mean candidates per column (no sizer)
+  int64_t slot_entries = 0;
+};
+
+constexpr int kTuneShapes[] = {1, 2, 4, 8};
+
+}  // namespace
+
+struct vo_batch {
+  int n = 0;
+  std::vector<int> ops;
+  std::vector<double> radii;
+  std::vector<const vo_volume *> ins;
+  std::vector<vo_volume *> normalized;  // owned copies of inputs with inverted pairs rewritten
+  std::vector<Launch> rec;             // recorded device steps, in order
+  size_t executed = 0;                 // closures already run eagerly
+  int kernels = 0;                     // kernel launches per replay
+  std::vector<void *> dmem;            // device allocations of the plan
+  std::vector<SlotVol> owned;
+  std::vector<SlotVol> finals;
+  int *d_flags = nullptr;  // [v]: overflow of volume v, [n]: complement slot overflow
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<vo_volume *> rerun;
+  vo_batch_stats stats{};
+};
+
+namespace {
+
+template <typename T>
+int plan_alloc(vo_ctx *ctx, vo_batch *b, T **p, size_t n) {
+  int rc = dalloc(ctx, p, n);
+  if (!rc) b->dmem.push_back((void *)*p);
+  return rc;
+}
+
+// Runs the recorded closures not yet run.
+void run_pending(vo_ctx *ctx, vo_batch *b) {
+  for (; b->executed < b->rec.size(); ++b->executed) b->rec[b->executed](ctx->stream);
+}
+
+void record(vo_batch *b, int kernels, Launch f) {
+  b->rec.push_back(std::move(f));
+  b->kernels += kernels;
+}
+
+// Maximum segment count of a slot volume (synchronising).
+int max_count(vo_ctx *ctx, const SlotVol &v, int *out) {
+  int *d = nullptr;
+  int rc = dalloc(ctx, &d, 1);
+  if (rc) return rc;
+  cudaMemsetAsync(d, 0, sizeof(int), ctx->stream);
+  slot_max_count(ctx, v, d);
+  int h = 0;
+  cudaMemcpyAsync(&h, d, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+  dfree(ctx, d);
+  VO_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  *out = h;
+  return VO_OK;
+}
+
+// Output slot layout of one dilation: learned per-tile capacities, or fixed.
+int size_output(vo_ctx *ctx, vo_batch *b, DilPlan &d, double radius) {
+  const vo_grid &g = d.in.grid;
+  const int ncols = g.nx * g.ny;
+  d.tiles32_x = (g.nx + kSizerTile - 1) / kSizerTile;
+  d.tiles32 = d.tiles32_x * ((g.ny + kSizerTile - 1) / kSizerTile);
+  int rc = VO_OK;
+  int64_t entries = (int64_t)ncols * kUnionCap;
+  if (ctx->sizer) {
+    float *feats = nullptr, *pred = nullptr;
+    int nt = 0;
+    rc = dalloc(ctx, &feats, (size_t)d.tiles32 * VO_SIZER_FEATURES);
+    if (!rc) rc = dalloc(ctx, &pred, (size_t)d.tiles32 * 4);
+    if (!rc) rc = sizer_features_device(ctx, d.in, radius, feats, &nt);
+    if (!rc) rc = sizer_predict_device(ctx, ctx->sizer, feats, nt, pred);
+    std::vector<float> hp((size_t)d.tiles32 * 4);
+    if (!rc) {
+      cudaMemcpyAsync(hp.data(), pred, sizeof(float) * hp.size(), cudaMemcpyDeviceToHost, ctx->stream);
+      cudaError_t e = cudaStreamSynchronize(ctx->stream);
+      if (e != cudaSuccess) rc = cuda_error(ctx, e, "sizer prediction");
+    }
+    dfree(ctx, feats);
+    dfree(ctx, pred);
+    if (rc) return rc;
+    std::vector<int32_t> cap(d.tiles32), off(d.tiles32);
+    d.tile_work.resize(d.tiles32);
+    int64_t total = 0;
+    for (int t = 0; t < d.tiles32; ++t) {
+      const int tx = t % d.tiles32_x, ty = t / d.tiles32_x;
+      const int cols = std::min(kSizerTile, g.nx - tx * kSizerTile) * std::min(kSizerTile, g.ny - ty * kSizerTile);
+      // predicted max segments per column, with a margin against the error of a log2 estimate
+      const double mx = std::exp2((double)hp[(size_t)t * 4]) - 1.0;
+      const int c = (int)std::min<double>(kUnionCapMid, std::max(1.0, std::ceil(mx * 1.25 + 2.0)));
+      cap[t] = c;
+      off[t] = (int32_t)total;
+      total += (int64_t)c * cols;
+      const double w = std::exp2((double)hp[(size_t)t * 4 + 2]) - 1.0;
+      d.tile_work[t] = w >= 0 && w < 1e30 ? (float)w : 0.f;  // a diverged network must not break the sort
+    }
+    d.spill_base = (int)total;
+    d.spill_cap = (int)std::max<int64_t>(4096, total / 32);
+    entries = total + d.spill_cap;
+    if (entries > 2147483647LL) return set_error(ctx, VO_ERANGE, "batch: slot layout exceeds int32 offsets");
+    rc = plan_alloc(ctx, b, &d.tcap, (size_t)d.tiles32);
+    if (!rc) rc = plan_alloc(ctx, b, &d.toff, (size_t)d.tiles32);
+    if (!rc) rc = plan_alloc(ctx, b, &d.spill_used, 1);
+    if (rc) return rc;
+    cudaMemcpyAsync(d.tcap, cap.data(), sizeof(int32_t) * cap.size(), cudaMemcpyHostToDevice, ctx->stream);
+    cudaMemcpyAsync(d.toff, off.data(), sizeof(int32_t) * off.size(), cudaMemcpyHostToDevice, ctx->stream);
+    VO_CK(ctx, cudaStreamSynchronize(ctx->stream));  // the host vectors go out of scope
+  } else {
+    // fixed capacity kUnionCap per column, spill space for 1/8 of that
+    d.spill_base = (int)std::min<int64_t>(entries, 2147483647LL);
+    d.spill_cap = (int)std::max<int64_t>(4096, entries / 8);
+    entries += d.spill_cap;
+    if (entries > 2147483647LL) return set_error(ctx, VO_ERANGE, "batch: slot layout exceeds int32 offsets");
+    rc = plan_alloc(ctx, b, &d.spill_used, 1);
+    if (rc) return rc;
+  }
+  d.slot_entries = entries;
+  d.out = SlotVol();
+  d.out.grid = g;
+  d.out.cap = kUnionCap;
+  d.out.entries = entries;
+  d.out.owns = false;  // plan memory
+  rc = plan_alloc(ctx, b, &d.out.beg, (size_t)ncols);
+  if (!rc) rc = plan_alloc(ctx, b, &d.out.end, (size_t)ncols);
+  if (!rc) rc = plan_alloc(ctx, b, &d.out.z, (size_t)entries);
+  return rc;
+}
+
+BatchVol batch_vol(const DilPlan &d, int *ovf) {
+  BatchVol v;
+  const vo_grid &g = d.in.grid;
+  v.A = FastArgs{g.nx, g.ny, d.T->host.W, d.in.beg, d.in.end, (const double *)d.in.z, d.zf, d.T->Hf, d.T->H,
+                 d.pairs, d.npairs, d.E, d.dom, d.segdom, d.T->dH, (d.T->host.Dy + 1) * d.T->host.W};
+  v.obeg = d.out.beg;
+  v.oend = d.out.end;
+  v.oz = d.out.z;
+  v.tcap = d.tcap;
+  v.toff = d.toff;
+  v.cap = kUnionCap;
+  v.tiles32_x = d.tiles32_x;
+  v.spill_base = d.spill_base;
+  v.spill_cap = d.spill_cap;
+  v.spill_used = d.spill_used;
+  v.mid_list = d.mid_list;
+  v.mid_count = d.mid_count;
+  v.ovf = ovf;
+  return v;
+}
+
+// Work queue for blocks of kFastCols x fby columns, in decreasing estimated work.
+std::vector<int2> build_queue(const std::vector<DilPlan> &dils, int fby) {
+  struct Item {
+    float w;
+    int2 q;
+  };
+  std::vector<Item> items;
+  for (size_t i = 0; i < dils.size(); ++i) {
+    const DilPlan &d = dils[i];
+    const vo_grid &g = d.in.grid;
+    const int tx = (g.nx + kFastCols - 1) / kFastCols, ty = (g.ny + fby - 1) / fby;
+    for (int t = 0; t < tx * ty; ++t) {
+      float w = (float)d.cost;
+      if (!d.tile_work.empty()) {
+        const int x = (t % tx) * kFastCols, y = (t / tx) * fby;
+        w = d.tile_work[(x / kSizerTile) + d.tiles32_x * (y / kSizerTile)];
+      }
+      items.push_back(Item{w, make_int2((int)i, t)});
+    }
+  }
+  std::stable_sort(items.begin(), items.end(), [](const Item &a, const Item &b) { return a.w > b.w; });
+  std::vector<int2> q(items.size());
+  for (size_t i = 0; i < items.size(); ++i) q[i] = items[i].q;
+  return q;
+}
+
+int sm_count() {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms > 0 ? sms : 1;
+}
+
+// Autotuner: times every block shape on an evenly strided sample of the
+// round's queue (about 1/16 of it, at least 512 items) and keeps the fastest
+// per column. Results are cached in the context per (log2 columns, radius
+// bucket, learned or not). Tuning launches write into the round's output
+// slots, which the real launch overwrites.
+int tune_shape(vo_ctx *ctx, vo_batch *b, const std::vector<DilPlan> &dils, const BatchVol *dvols,
+               int *fby_out) {
+  int64_t cols = 0;
+  double rmax = 0;
+  for (const DilPlan &d : dils) {
+    cols += (int64_t)d.in.grid.nx * d.in.grid.ny;
+    rmax = std::max(rmax, b->radii[d.vol]);
+  }
+  const long long key = ((long long)std::ilogb((double)std::max<int64_t>(cols, 1)) << 16) |
+                        ((long long)(rmax / 8) << 1) | (ctx->sizer ? 1 : 0);
+  for (const auto &kv : ctx->tune_cache)
+    if (kv.first == key) {
+      *fby_out = kv.second;
+      return VO_OK;
+    }
+  const int sms = sm_count();
+  int best = 4;
+  double best_t = 1e300;
+  int *dnext = nullptr;
+  int2 *dq = nullptr;
+  int rc = dalloc(ctx, &dnext, 1);
+  size_t qcap = 0;
+  for (int fby : kTuneShapes) {
+    if (rc) break;
+    const int per_sm = fast_batched_blocks_per_sm(fby);
+    if (per_sm <= 0) continue;
+    const std::vector<int2> full = build_queue(dils, fby);
+    const size_t want = std::max<size_t>(512, full.size() / 16);
+    const size_t stride = std::max<size_t>(1, full.size() / want);
+    std::vector<int2> sample;
+    for (size_t i = 0; i < full.size(); i += stride) sample.push_back(full[i]);
+    if (sample.size() > qcap) {
+      dfree(ctx, dq);
+      qcap = sample.size();
+      rc = dalloc(ctx, &dq, qcap);
+      if (rc) break;
+    }
+    cudaMemcpyAsync(dq, sample.data(), sizeof(int2) * sample.size(), cudaMemcpyHostToDevice, ctx->stream);
+    const int grid = std::max(1, std::min<int>((int)sample.size(), sms * per_sm));
+    float ms = 0;
+    for (int rep = 0; rep < 2; ++rep) {  // the first run warms caches and clocks
+      cudaMemsetAsync(dnext, 0, sizeof(int), ctx->stream);
+      for (const DilPlan &d : dils) {
+        cudaMemsetAsync(d.spill_used, 0, sizeof(int), ctx->stream);
+        cudaMemsetAsync(d.mid_count, 0, sizeof(int), ctx->stream);
+      }
+      cudaEventRecord(ctx->ev[2], ctx->stream);
+      fast_batched_launch(fby, grid, ctx->stream, dvols, dq, (int)sample.size(), dnext);
+      cudaEventRecord(ctx->ev[3], ctx->stream);
+      cudaError_t e = cudaStreamSynchronize(ctx->stream);
+      if (e != cudaSuccess) {
+        rc = cuda_error(ctx, e, "autotune");
+        break;
+      }
+      cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]);
+    }
+    if (rc) break;
+    const double per_col = ms / ((double)sample.size() * kFastCols * fby);
+    b->stats.tune_ms[fby == 1 ? 0 : fby == 2 ? 1 : fby == 4 ? 2 : 3] = ms;
+    if (per_col < best_t) {
+      best_t = per_col;
+      best = fby;
+    }
+  }
+  dfree(ctx, dnext);
+  dfree(ctx, dq);
+  if (rc) return rc;
+  ctx->tune_cache.push_back({key, best});
+  *fby_out = best;
+  return VO_OK;
+}
+
+int plan_dilation_round(vo_ctx *ctx, vo_batch *b, std::vector<DilPlan> &dils, bool later_rounds) {
+  const int sms = sm_count();
+  int rc = VO_OK;
+  for (DilPlan &d : dils) {
+    const vo_grid &g = d.in.grid;
+    const int ncols = g.nx * g.ny;
+    const std::vector<int2> pairs = fast_pairs(d.T->host);
+    d.npairs = (int)pairs.size();
+    rc = plan_alloc(ctx, b, &d.zf, 2 * (size_t)std::max<int64_t>(d.in.entries, 1));
+    if (!rc) rc = plan_alloc(ctx, b, &d.E, 1);
+    if (!rc) rc = plan_alloc(ctx, b, &d.dom, (size_t)4 * ncols);
+    if (!rc) rc = plan_alloc(ctx, b, &d.segdom, (size_t)std::max<int64_t>(d.in.entries, 1));
+    if (!rc) rc = plan_alloc(ctx, b, &d.mid_list, (size_t)ncols);
+    if (!rc) rc = plan_alloc(ctx, b, &d.mid_count, 1);
+    if (!rc) rc = plan_alloc(ctx, b, &d.maxbits, 1);
+    if (!rc) rc = plan_alloc(ctx, b, &d.pairs, pairs.size());
+    if (rc) return rc;
+    cudaMemcpyAsync(d.pairs, pairs.data(), sizeof(int2) * pairs.size(), cudaMemcpyHostToDevice, ctx->stream);
+    VO_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    const SlotVol in = d.in;
+    float *zf = d.zf, *E = d.E, *dom = d.dom;
+    float4 *segdom = d.segdom;
+    unsigned int *mb = d.maxbits;
+    const float R = (float)b->radii[d.vol];
+    record(b, 3, [in, zf, E, mb, R, dom, segdom](cudaStream_t st) {
+      fast_prepare(st, in.grid.nx, in.grid.ny, in.beg, in.end, in.z, zf, mb, R, E, dom, segdom);
+    });
+    // candidates per column ~ 4 x pairs x mean segments of the input (no sizer)
+    const double segs = d.in.cap > 0 && d.in.owns ? d.in.cap * 0.5 : (double)d.in.entries / std::max(ncols, 1);
+    d.cost = (double)d.npairs * 4.0 * (segs + 0.5);
+  }
+  if (ctx->sizer) run_pending(ctx, b);  // features need the dilation inputs
+  for (DilPlan &d : dils) {
+    rc = size_output(ctx, b, d, b->radii[d.vol]);
+    if (rc) return rc;
+    b->stats.slot_bytes += d.slot_entries * (int64_t)sizeof(double2);
+  }
+  std::vector<BatchVol> hv;
+  for (DilPlan &d : dils) hv.push_back(batch_vol(d, b->d_flags + d.vol));
+  BatchVol *dvols = nullptr;
+  int *dnext = nullptr;
+  rc = plan_alloc(ctx, b, &dvols, hv.size());
+  if (!rc) rc = plan_alloc(ctx, b, &dnext, 1);
+  if (rc) return rc;
+  cudaMemcpyAsync(dvols, hv.data(), sizeof(BatchVol) * hv.size(), cudaMemcpyHostToDevice, ctx->stream);
+  VO_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  int fby = 4;
+  run_pending(ctx, b);  // tuning reads the dilation inputs
+  rc = tune_shape(ctx, b, dils, dvols, &fby);
+  if (rc) return rc;
+  const std::vector<int2> q = build_queue(dils, fby);
+  int2 *dq = nullptr;
+  rc = plan_alloc(ctx, b, &dq, q.size());
+  if (rc) return rc;
+  cudaMemcpyAsync(dq, q.data(), sizeof(int2) * q.size(), cudaMemcpyHostToDevice, ctx->stream);
+  VO_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  const int per_sm = std::max(1, fast_batched_blocks_per_sm(fby));
+  const int grid = std::max(1, std::min<int>((int)q.size(), sms * per_sm));
+  std::vector<int *> counters;  // reset before every replay
+  for (DilPlan &d : dils) {
+    counters.push_back(d.spill_used);
+    counters.push_back(d.mid_count);
+  }
+  const int nq = (int)q.size(), nv = (int)dils.size(), gmid = sms * 16;
+  record(b, 2, [=](cudaStream_t st) {
+    cudaMemsetAsync(dnext, 0, sizeof(int), st);
+    for (int *s : counters) cudaMemsetAsync(s, 0, sizeof(int), st);
+    fast_batched_launch(fby, grid, st, dvols, dq, nq, dnext);
+    fast_batched_mid_launch(st, dvols, nv, gmid);
+  });
+  b->stats.tile_rows = fby;
+  b->stats.tiles += nq;
+  if (later_rounds) run_pending(ctx, b);
+  return VO_OK;
+}
+
+void plan_free(vo_ctx *ctx, vo_batch *b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  for (SlotVol &s : b->owned) slot_free(ctx, s);
+  for (void *p : b->dmem) dfree(ctx, p);
+  for (vo_volume *v : b->normalized)
+    if (v) vo_volume_free(ctx, v);
+  for (vo_volume *v : b->rerun)
+    if (v) vo_volume_free(ctx, v);
+  cudaStreamSynchronize(ctx->stream);
+  delete b;
+}
+
+int plan_build(vo_ctx *ctx, vo_batch *b) {
+  const int n = b->n;
+  int rc = plan_alloc(ctx, b, &b->d_flags, (size_t)n + 1);
+  if (rc) return rc;
+  int *flags = b->d_flags;
+  record(b, 0, [flags, n](cudaStream_t st) { cudaMemsetAsync(flags, 0, sizeof(int) * (n + 1), st); });
+  std::vector<std::vector<StepKind>> chain(n);
+  std::vector<SlotVol> cur(n);
+  std::vector<const DeviceTables *> tabs(n);
+  for (int v = 0; v < n; ++v) {
+    chain[v] = steps_of(b->ops[v]);
+    const vo_volume *in = b->ins[v];
+    if (chain[v][0] == kDil) {  // inverted pairs in a dilation input are rewritten first
+      rc = normalize_inverted(ctx, in, &b->normalized[v]);
+      if (rc) return rc;
+      if (b->normalized[v]) in = b->normalized[v];
+    }
+    cur[v] = slot_view(in, 0);
+    rc = max_count(ctx, cur[v], &cur[v].cap);
+    if (!rc) rc = get_tables(ctx, b->radii[v], std::max(in->grid.nx, in->grid.ny) + 2, &tabs[v]);
+    if (rc) return rc;
+  }
+  std::vector<size_t> next(n, 0);
+  for (;;) {
+    std::vector<DilPlan> dils;
+    bool any = false;
+    for (int v = 0; v < n; ++v) {
+      if (next[v] >= chain[v].size()) continue;
+      any = true;
+      const StepKind k = chain[v][next[v]++];
+      const SlotVol in = cur[v];
+      SlotVol out;
+      int *ovf = b->d_flags + n;
+      if (k == kDil) {
+        DilPlan d;
+        d.vol = v;
+        d.in = in;
+        d.T = tabs[v];
+        dils.push_back(d);
+        continue;
+      }
+      // complement steps: slot outputs sized from the input's largest column
+      if (k == kNeg) {
+        vo_grid g2 = in.grid;
+        g2.nx += 2;
+        g2.ny += 2;
+        rc = slot_alloc(ctx, g2, in.cap + 1, out);
+        if (!rc) record(b, 1, [in, out, ovf](cudaStream_t st) { slot_negate_launch(st, in, out, ovf); });
+      } else if (k == kNorm) {
+        rc = slot_alloc(ctx, in.grid, in.cap + 2, out);
+        if (!rc) record(b, 1, [in, out, ovf](cudaStream_t st) { slot_normalize_launch(st, in, out, ovf); });
+      } else {
+        const vo_grid g = b->ins[v]->grid;
+        rc = slot_alloc(ctx, g, in.cap + 1, out);
+        if (!rc) record(b, 1, [in, g, out, ovf](cudaStream_t st) { slot_negate_inv_launch(st, in, g, out, ovf); });
+      }
+      if (rc) return rc;
+      b->owned.push_back(out);
+      cur[v] = out;
+    }
+    if (!any) break;
+    if (dils.empty()) continue;
+    bool later = false;
+    for (const DilPlan &d : dils) later |= next[d.vol] < chain[d.vol].size();
+    rc = plan_dilation_round(ctx, b, dils, later);
+    if (rc) return rc;
+    for (DilPlan &d : dils) {
+      cur[d.vol] = d.out;
+      // a complement of this result needs its largest column (the data exists: the round ran)
+      if (next[d.vol] < chain[d.vol].size()) {
+        rc = max_count(ctx, d.out, &cur[d.vol].cap);
+        if (rc) return rc;
+      }
+    }
+  }
+  b->finals = cur;
+  // ---- capture every recorded step into one graph
+  VO_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  VO_CK(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  for (Launch &f : b->rec) f(ctx->stream);
+  cudaError_t e = cudaStreamEndCapture(ctx->stream, &b->graph);
+  if (e != cudaSuccess) return cuda_error(ctx, e, "graph capture");
+  e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+  if (e != cudaSuccess) return cuda_error(ctx, e, "graph instantiate");
+  size_t nodes = 0;
+  cudaGraphGetNodes(b->graph, nullptr, &nodes);
+  b->stats.graph_nodes = (int)nodes;
+  b->stats.graph_kernels = b->kernels;
+  b->stats.learned = ctx->sizer ? 1 : 0;
+  return VO_OK;
+}
+
+// Single-volume re-run of volume v (any union size).
+int rerun_volume(vo_ctx *ctx, vo_batch *b, int v, vo_volume **out) {
+  vo_timings t;
+  std::memset(&t, 0, sizeof t);
+  const vo_volume *in = b->ins[v];
+  const double r = b->radii[v];
+  switch (b->ops[v]) {
+    case VO_DILATION:
+      return dilate(ctx, VO_METHOD_FAST, r, in, out, &t);
+    case VO_EROSION:
+      return erode(ctx, VO_METHOD_FAST, r, in, out, &t);
+    default: {
+      vo_volume *tmp = nullptr;
+      const bool open = b->ops[v] == VO_OPENING;
+      int rc = open ? erode(ctx, VO_METHOD_FAST, r, in, &tmp, &t) : dilate(ctx, VO_METHOD_FAST, r, in, &tmp, &t);
+      if (!rc) rc = open ? dilate(ctx, VO_METHOD_FAST, r, tmp, out, &t) : erode(ctx, VO_METHOD_FAST, r, tmp, out, &t);
+      if (tmp) vo_volume_free(ctx, tmp);
+      return rc;
+    }
+  }
+}
+
+int volume_copy(vo_ctx *ctx, const vo_volume *src, vo_volume **out) {
+  vo_volume *v = nullptr;
+  int rc = volume_alloc(ctx, src->grid, src->nseg, &v);
+  if (rc) return rc;
+  const size_t ncols = (size_t)src->grid.nx * src->grid.ny;
+  cudaMemcpyAsync(v->offs, src->offs, sizeof(int32_t) * (ncols + 1), cudaMemcpyDeviceToDevice, ctx->stream);
+  if (src->nseg > 0)
+    cudaMemcpyAsync(v->z, src->z, sizeof(double2) * src->nseg, cudaMemcpyDeviceToDevice, ctx->stream);
+  v->inverted = src->inverted;
+  *out = v;
+  return VO_OK;
+}
+
+bool valid_batch(int n, const int *ops, const double *radii, int method, const vo_volume *const *ins) {
+  if (n < 0 || (n > 0 && (!ops || !radii || !ins))) return false;
+  if (method != VO_METHOD_FAST) return false;
+  for (int i = 0; i < n; ++i)
+    if (!ins[i] || ops[i] < VO_DILATION || ops[i] > VO_CLOSING || !(radii[i] >= 0) || radii[i] > 255) return false;
+  return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+int vo_batch_create(vo_ctx *ctx, int n, const int *ops, const double *radii, int method,
+                    const vo_volume *const *ins, vo_batch **out) {
+  if (!ctx || !out) return VO_EINVAL;
+  *out = nullptr;
+  if (!valid_batch(n, ops, radii, method, ins))
+    return set_error(ctx, VO_EINVAL, "batch: bad volume, op, radius or method (VO_METHOD_FAST only)");
+  cudaSetDevice(ctx->device);
+  ctx->err.clear();
+  const auto t0 = std::chrono::steady_clock::now();
+  vo_batch *b = new vo_batch();
+  b->n = n;
+  b->ops.assign(ops, ops + n);
+  b->radii.assign(radii, radii + n);
+  b->ins.assign(ins, ins + n);
+  b->normalized.assign(n, nullptr);
+  b->rerun.assign(n, nullptr);
+  std::memset(&b->stats, 0, sizeof b->stats);
+  const int rc = plan_build(ctx, b);
+  if (rc) {
+    cudaStreamSynchronize(ctx->stream);
+    cudaGetLastError();
+    plan_free(ctx, b);
+    return rc;
+  }
+  b->stats.plan_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  *out = b;
+  return VO_OK;
+}
+
+int vo_batch_run(vo_ctx *ctx, vo_batch *b, vo_timings *tm) {
+  if (!ctx || !b) return VO_EINVAL;
+  cudaSetDevice(ctx->device);
+  const auto t0 = std::chrono::steady_clock::now();
+  for (vo_volume *&v : b->rerun)
+    if (v) {
+      vo_volume_free(ctx, v);
+      v = nullptr;
+    }
+  const int n = b->n;
+  std::vector<int> flags(n + 1, 0);
+  cudaEventRecord(ctx->ev[0], ctx->stream);
+  VO_CK(ctx, cudaGraphLaunch(b->exec, ctx->stream));
+  cudaEventRecord(ctx->ev[1], ctx->stream);
+  cudaMemcpyAsync(flags.data(), b->d_flags, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, ctx->stream);
+  VO_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  float graph_ms = 0;
+  cudaEventElapsedTime(&graph_ms, ctx->ev[0], ctx->ev[1]);
+  int reruns = 0;
+  const int launches0 = ctx->launches;
+  for (int v = 0; v < n; ++v) {
+    if (!flags[v] && !flags[n]) continue;
+    ++reruns;
+    const int rc = rerun_volume(ctx, b, v, &b->rerun[v]);
+    if (rc) return rc;
+  }
+  b->stats.reruns = reruns;
+  if (tm) {
+    std::memset(tm, 0, sizeof *tm);
+    tm->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    tm->pass2_ms = graph_ms;
+    tm->kernel_ms[3] = graph_ms;
+    for (int v = 0; v < n; ++v) tm->in_segments += b->ins[v]->nseg;
+    tm->kernel_launches = b->kernels + (ctx->launches - launches0);
+    tm->overflow_columns = reruns;
+  }
+  return VO_OK;
+}
+
+int vo_batch_outputs(vo_ctx *ctx, vo_batch *b, vo_volume **outs) {
+  if (!ctx || !b || (b->n > 0 && !outs)) return VO_EINVAL;
+  cudaSetDevice(ctx->device);
+  int rc = VO_OK;
+  for (int v = 0; v < b->n; ++v) outs[v] = nullptr;
+  for (int v = 0; v < b->n && !rc; ++v)
+    rc = b->rerun[v] ? volume_copy(ctx, b->rerun[v], &outs[v]) : slot_to_volume(ctx, b->finals[v], &outs[v]);
+  if (!rc) {
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) rc = cuda_error(ctx, e, "batch outputs");
+  }
+  if (rc)
+    for (int v = 0; v < b->n; ++v)
+      if (outs[v]) {
+        vo_volume_free(ctx, outs[v]);
+        outs[v] = nullptr;
+      }
+  return rc;
+}
+
+int vo_batch_stats_get(vo_ctx *ctx, const vo_batch *b, vo_batch_stats *s) {
+  if (!ctx || !b || !s) return VO_EINVAL;
+  *s = b->stats;
+  return VO_OK;
+}
+
+void vo_batch_destroy(vo_ctx *ctx, vo_batch *b) {
+  if (!ctx || !b) return;
+  cudaSetDevice(ctx->device);
+  plan_free(ctx, b);
+}
+
+}  // extern "C"
+
+namespace vo {
+
+int morph_batched_fast(vo_ctx *ctx, int n, const int *ops, const double *radii, const vo_volume *const *ins,
+                       vo_volume **outs, vo_timings *tm) {
+  const auto t0 = std::chrono::steady_clock::now();
+  vo_batch *b = nullptr;
+  int rc = vo_batch_create(ctx, n, ops, radii, VO_METHOD_FAST, ins, &b);
+  if (rc) return rc;
+  rc = vo_batch_run(ctx, b, tm);
+  if (!rc) rc = vo_batch_outputs(ctx, b, outs);
+  if (!rc && tm) {
+    tm->total_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    for (int v = 0; v < n; ++v) tm->out_segments += outs[v]->nseg;
+  }
+  vo_batch_destroy(ctx, b);
+  return rc;
+}
+
+}  // namespace vo

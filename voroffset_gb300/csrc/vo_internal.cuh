@@ -51,6 +51,11 @@ struct DeviceTables {
   float *Hf = nullptr;
   int *Dx = nullptr;
   double *HB = nullptr;
+  // FP32 lower bounds of the growth of H one lattice step toward the centre:
+  // dH[d*W + a] <= H[d][a-1] - H[d][a] (x step, a >= 1) and
+  // dH[(Dy+1)*W + d*W + a] <= H[d-1][a] - H[d][a] (y step, d >= 1); -inf where
+  // no step exists (used by the dominance test of the FP32 kernels).
+  float *dH = nullptr;
   Tables host;
   DevTables view() const { return DevTables{host.Dy, host.W, H, Hf, Dx, HB}; }
 };
@@ -80,6 +85,8 @@ struct vo_ctx {
   int *d_flags = nullptr;  // [0]: overflow count, [1..]: misc status
   long long *d_total = nullptr;
   long long *h_total = nullptr;  // pinned
+  vo_sizer *sizer = nullptr;     // learned sizing for the batched executor (not owned)
+  std::vector<std::pair<long long, int>> tune_cache;  // batch autotuner: shape key -> rows per block
 };
 
 namespace vo {
@@ -127,11 +134,14 @@ int dilate(vo_ctx *ctx, int method, double R, const vo_volume *in, vo_volume **o
 int erode(vo_ctx *ctx, int method, double R, const vo_volume *in, vo_volume **out,
           vo_timings *tm);
 
-// Fixed-capacity slot volume: column c at z[c*cap, end[c]), beg[c] = c*cap;
-// a CSR volume is viewed as one with beg = offs, end = offs + 1.
+// Slot volume: column c holds z[beg[c], end[c]). slot_alloc gives the
+// fixed-capacity layout beg[c] = c*cap; a CSR volume is viewed as one with
+// beg = offs, end = offs + 1; batch dilations write per-tile layouts. `cap`
+// bounds every column's count, `entries` is the length of z.
 struct SlotVol {
   vo_grid grid{};
   int cap = 0;
+  int64_t entries = 0;
   int32_t *beg = nullptr, *end = nullptr;
   double2 *z = nullptr;
   bool owns = false;
@@ -143,12 +153,80 @@ void slot_end_from_counts(vo_ctx *ctx, SlotVol &v, const int32_t *counts);
 int slot_negate(vo_ctx *ctx, const SlotVol &in, SlotVol &out, int *overflow);
 int slot_normalize(vo_ctx *ctx, const SlotVol &in, SlotVol &out, int *overflow);
 int slot_negate_inv(vo_ctx *ctx, const SlotVol &in, const vo_grid &g, SlotVol &out, int *overflow);
+// The same three steps as launches only, into already allocated outputs
+// (for graph capture).
+void slot_negate_launch(cudaStream_t st, const SlotVol &in, const SlotVol &out, int *overflow);
+void slot_normalize_launch(cudaStream_t st, const SlotVol &in, const SlotVol &out, int *overflow);
+void slot_negate_inv_launch(cudaStream_t st, const SlotVol &in, const vo_grid &g, const SlotVol &out,
+                            int *overflow);
 int slot_max_count(vo_ctx *ctx, const SlotVol &v, int *d_max);
 int slot_to_volume(vo_ctx *ctx, const SlotVol &v, vo_volume **out);
 
-// Batched executor (vo_fast.cu).
+// Arguments of the FP32-guarded dilation of one volume (vo_fast.cu).
+struct FastArgs {
+  int nx, ny, W;
+  // Column c's segments are [beg[c], end[c]); for CSR input beg = offs and
+  // end = offs + 1, for a slot layout beg / end are the slot arrays.
+  const int32_t *beg, *end;
+  const double *zd;     // FP64 values, 2 per segment
+  const float *zf;      // FP32 copies
+  const float *Hf;      // [(Dy+1) * W]
+  const double *H64;    // [(Dy+1) * W]
+  const int2 *pairs;    // (a, d) sorted by decreasing H
+  int npairs;
+  const float *E;       // guard band (device scalar)
+  const float *dom;       // [4][ncols] column dominance widths (fast_prepare), or nullptr
+  const float4 *segdom;   // per segment dominance widths (x-, x+, y-, y+), or nullptr
+  const float *dH;        // DeviceTables::dH
+  int dHy;                // offset of the y-step half of dH: (Dy+1) * W
+};
+
+// One dilation of a batch (device array element of the persistent kernel).
+constexpr int kSizerTile = 32;  // side of a sizing tile (columns)
+constexpr int kUnionCap = 32;      // union capacity of the main FP32 kernels
+constexpr int kUnionCapMid = 128;  // union capacity of their second tier
+struct BatchVol {
+  FastArgs A;
+  int32_t *obeg, *oend;  // output slot arrays, written for every column
+  double2 *oz;           // output values: tile slots, then the spill region
+  const int32_t *tcap;   // per sizing tile capacity, or nullptr: `cap` for all
+  const int32_t *toff;   // per sizing tile offset into oz
+  int cap;
+  int tiles32_x;
+  int spill_base, spill_cap;
+  int *spill_used;
+  int *mid_list, *mid_count;  // columns whose union exceeds kUnionCap (second tier)
+  int *ovf;  // set when a column's union does not fit (slot + spill, or kUnionCapMid)
+};
+
+// Fills DeviceTables::dH from H on the device (directed rounding).
+void launch_dh_tables(cudaStream_t st, int Dy, int W, const double *H, const int *Dx, float *dH);
+
+// (a, d) pairs with a <= Dx[d], sorted by decreasing H (the candidate order of
+// the FP32 kernels).
+std::vector<int2> fast_pairs(const Tables &h);
+// FP32 copies of the values of a slot volume, the guard band scalar, and (dom
+// not null) the dominance widths: per column and direction (x-, x+, y-, y+)
+// into dom[4][ncols], per segment into segdom (may be null).
+void fast_prepare(cudaStream_t st, int nx, int ny, const int32_t *beg, const int32_t *end, const double2 *z,
+                  float *zf, unsigned int *maxbits, float R, float *E, float *dom, float4 *segdom);
+// Launch of the persistent kernel with `fby` rows of kFB columns per block
+// (fby in {1, 2, 4, 8}); blocks_per_sm is the occupancy for that shape.
+int fast_batched_launch(int fby, int grid, cudaStream_t st, const BatchVol *vols, const int2 *queue, int nq,
+                        int *next);
+int fast_batched_blocks_per_sm(int fby);
+// Second tier of a batch round over the dilations vols[0..nv) (grid-stride).
+void fast_batched_mid_launch(cudaStream_t st, const BatchVol *vols, int nv, int grid);
+constexpr int kFastCols = 32;  // columns per block row
+
+// Batch plans (vo_batch.cu).
 int morph_batched_fast(vo_ctx *ctx, int n, const int *ops, const double *radii, const vo_volume *const *ins,
                        vo_volume **outs, vo_timings *tm);
+
+// Learned sizing (vo_sizer.cu): tile features of a slot volume into a device
+// array of ntiles x VO_SIZER_FEATURES, and predictions (ntiles x 4, three used).
+int sizer_features_device(vo_ctx *ctx, const SlotVol &in, double radius, float *feats, int *ntiles);
+int sizer_predict_device(vo_ctx *ctx, const vo_sizer *s, const float *feats, int n, float *out4);
 
 // Volume allocation (vo_api.cu).
 int volume_alloc(vo_ctx *ctx, const vo_grid &g, int64_t nseg, vo_volume **out);

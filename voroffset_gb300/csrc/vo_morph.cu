@@ -1237,6 +1237,7 @@ int slot_alloc(vo_ctx *ctx, const vo_grid &g, int cap, SlotVol &v) {
   v.grid = g;
   v.cap = cap;
   const int ncols = g.nx * g.ny;
+  v.entries = (int64_t)ncols * std::max(cap, 1);
   int rc = dalloc(ctx, &v.beg, (size_t)ncols);
   if (!rc) rc = dalloc(ctx, &v.end, (size_t)ncols);
   if (!rc) rc = dalloc(ctx, &v.z, (size_t)ncols * (size_t)std::max(cap, 1));
@@ -1266,6 +1267,7 @@ SlotVol slot_view(const vo_volume *in, int cap) {
   v.beg = in->offs;
   v.end = in->offs + 1;
   v.z = in->z;
+  v.entries = in->nseg;
   v.owns = false;
   return v;
 }
@@ -1276,38 +1278,50 @@ void slot_end_from_counts(vo_ctx *ctx, SlotVol &v, const int32_t *counts) {
   ctx->launches += 1;
 }
 
-int slot_negate(vo_ctx *ctx, const SlotVol &in, SlotVol &out, int *overflow) {
+void slot_negate_launch(cudaStream_t st, const SlotVol &in, const SlotVol &out, int *overflow) {
   const vo_grid &g = in.grid;
   const double zmin = g.origin[2] / g.spacing - 1;
   const double zmax = g.origin[2] / g.spacing + 2 * g.padding + g.extent[2] / g.spacing + 1;
-  vo_grid g2 = g;
+  k_negate_slot<<<nblocks((int64_t)(g.nx + 2) * (g.ny + 2), 256), 256, 0, st>>>(
+      g.nx, g.ny, in.beg, in.end, in.z, zmin, zmax, out.cap, out.end, out.z, overflow);
+}
+
+int slot_negate(vo_ctx *ctx, const SlotVol &in, SlotVol &out, int *overflow) {
+  vo_grid g2 = in.grid;
   g2.nx += 2;
   g2.ny += 2;
   int rc = slot_alloc(ctx, g2, in.cap + 1, out);
   if (rc) return rc;
-  k_negate_slot<<<nblocks((int64_t)g2.nx * g2.ny, 256), 256, 0, ctx->stream>>>(
-      g.nx, g.ny, in.beg, in.end, in.z, zmin, zmax, out.cap, out.end, out.z, overflow);
+  slot_negate_launch(ctx->stream, in, out, overflow);
   ctx->launches += 1;
   return VO_OK;
+}
+
+void slot_normalize_launch(cudaStream_t st, const SlotVol &in, const SlotVol &out, int *overflow) {
+  const int ncols = in.grid.nx * in.grid.ny;
+  k_norm_slot<<<nblocks(ncols, 128), 128, 0, st>>>(ncols, in.beg, in.end, in.z, out.cap, out.end, out.z, overflow);
 }
 
 int slot_normalize(vo_ctx *ctx, const SlotVol &in, SlotVol &out, int *overflow) {
   int rc = slot_alloc(ctx, in.grid, in.cap + 2, out);
   if (rc) return rc;
-  const int ncols = in.grid.nx * in.grid.ny;
-  k_norm_slot<<<nblocks(ncols, 128), 128, 0, ctx->stream>>>(ncols, in.beg, in.end, in.z, out.cap, out.end, out.z,
-                                                            overflow);
+  slot_normalize_launch(ctx->stream, in, out, overflow);
   ctx->launches += 1;
   return VO_OK;
 }
 
-int slot_negate_inv(vo_ctx *ctx, const SlotVol &in, const vo_grid &g, SlotVol &out, int *overflow) {
+void slot_negate_inv_launch(cudaStream_t st, const SlotVol &in, const vo_grid &g, const SlotVol &out,
+                            int *overflow) {
   const double zmin = g.origin[2] / g.spacing - 1;
   const double zmax = g.origin[2] / g.spacing + 2 * g.padding + g.extent[2] / g.spacing + 1;
+  k_negate_inv_slot<<<nblocks((int64_t)g.nx * g.ny, 256), 256, 0, st>>>(
+      g.nx, g.ny, in.beg, in.end, in.z, zmin + 1, zmax - 1, out.cap, out.end, out.z, overflow);
+}
+
+int slot_negate_inv(vo_ctx *ctx, const SlotVol &in, const vo_grid &g, SlotVol &out, int *overflow) {
   int rc = slot_alloc(ctx, g, in.cap + 1, out);
   if (rc) return rc;
-  k_negate_inv_slot<<<nblocks((int64_t)g.nx * g.ny, 256), 256, 0, ctx->stream>>>(
-      g.nx, g.ny, in.beg, in.end, in.z, zmin + 1, zmax - 1, out.cap, out.end, out.z, overflow);
+  slot_negate_inv_launch(ctx->stream, in, g, out, overflow);
   ctx->launches += 1;
   return VO_OK;
 }
