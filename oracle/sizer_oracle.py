@@ -7,7 +7,9 @@ what the device kernels compute:
 * forward: x[16] -> relu(x W1 + b1)[64] -> relu(h1 W2 + b2)[64] -> h2 W3 + b3[4],
   with every parameter rounded to BF16 (round to nearest even) first, as the
   device's inference weights are;
-* loss: mean over samples and the 3 used outputs of (out - target)^2;
+* loss: mean over samples and the 3 used outputs of w (out - target)^2, with
+  w = UNDER_WEIGHT where the first output (the max count) is below its target
+  and 1 elsewhere;
 * gradients of that loss with respect to every parameter, evaluated at the
   BF16-rounded parameters (the device trains FP32 master weights with the
   gradient of the BF16 network).
@@ -20,6 +22,7 @@ from __future__ import annotations
 import numpy as np
 
 NF, NH, NO, NUSED = 16, 64, 4, 3
+UNDER_WEIGHT = 4.0
 SHAPES = [("W1", (NF, NH)), ("b1", (NH,)), ("W2", (NH, NH)), ("b2", (NH,)), ("W3", (NH, NO)), ("b3", (NO,))]
 NPARAM = sum(int(np.prod(s)) for _, s in SHAPES)
 
@@ -59,7 +62,7 @@ def forward(params: np.ndarray, X: np.ndarray, quantize: bool = True):
 
 
 def loss_and_gradients(params: np.ndarray, X: np.ndarray, T: np.ndarray, quantize: bool = True):
-    """Mean squared error over the used outputs and its gradient (FP64)."""
+    """Weighted squared error over the used outputs and its gradient (FP64)."""
     p = bf16_round(params) if quantize else np.asarray(params, np.float32)
     P = {k: v.astype(np.float64) for k, v in unpack(p.astype(np.float64)).items()}
     X = np.asarray(X, np.float64)
@@ -68,8 +71,10 @@ def loss_and_gradients(params: np.ndarray, X: np.ndarray, T: np.ndarray, quantiz
     out, h1, h2, _, _ = forward(params, X, quantize)
     err = np.zeros_like(out)
     err[:, :NUSED] = out[:, :NUSED] - T
-    loss = float((err[:, :NUSED] ** 2).sum() / (n * NUSED))
-    dout = 2.0 * err / (n * NUSED)
+    w = np.ones_like(out)
+    w[:, 0] = np.where(err[:, 0] < 0, UNDER_WEIGHT, 1.0)
+    loss = float((w * err ** 2)[:, :NUSED].sum() / (n * NUSED))
+    dout = 2.0 * w * err / (n * NUSED)
     g = {"W3": h2.T @ dout, "b3": dout.sum(0)}
     dz2 = (dout @ P["W3"].T) * (h2 > 0)
     g["W2"] = h1.T @ dz2

@@ -134,11 +134,12 @@ def test_gpu_zero_length_and_touching_segments(ctx, vo, oracle, method):
 
 
 @pytest.mark.parametrize("method", METHODS)
-@pytest.mark.parametrize("k", [60, 150])
+@pytest.mark.parametrize("k", [40, 100, 150])
 def test_gpu_overflow_path(ctx, vo, oracle, method, k):
-    # many thin disjoint plates per column overflow the fast kernels' working
-    # lists (60: the 128-interval second tier of the FP32 method; 150: its
-    # FP64 list); the large-capacity re-runs must give the same answer
+    # many thin disjoint plates per column overflow the kernels' working lists
+    # (FP32 method: 40 fits its 64-interval variant for dense inputs, 100 needs
+    # the 128-interval second tier, 150 its FP64 list); the large-capacity
+    # re-runs must give the same answer
     nx, ny = 40, 40
     base = np.arange(k, dtype=np.float64) * 3.0
     z = np.stack([base, base + 1.0], 1).reshape(-1)
@@ -147,7 +148,8 @@ def test_gpu_overflow_path(ctx, vo, oracle, method, k):
     grid = vo.Grid(nx, ny, (0, 0, 0), (nx, ny, 3 * k), 1.0, 0)
     want = oracle.morph(ogrid(oracle, grid), offs, zz, 0.9, "dilation")
     got, t = run(ctx, grid, offs, zz, "dilation", 0.9, method)
-    assert t["overflow_columns"] > 0
+    if method != "fast" or k > 64:
+        assert t["overflow_columns"] > 0
     assert_same(got, want, tol=0.0)
 
 

@@ -32,7 +32,10 @@ def test_gradients_match_finite_differences():
         h1 = np.maximum(X @ P["W1"] + P["b1"], 0)
         h2 = np.maximum(h1 @ P["W2"] + P["b2"], 0)
         out = h2 @ P["W3"] + P["b3"]
-        return float(((out[:, :S.NUSED] - T) ** 2).sum() / (len(X) * S.NUSED))
+        e = out[:, :S.NUSED] - T
+        w = np.ones_like(e)
+        w[:, 0] = np.where(e[:, 0] < 0, S.UNDER_WEIGHT, 1.0)
+        return float((w * e ** 2).sum() / (len(X) * S.NUSED))
     assert abs(f(p.astype(np.float32).astype(np.float64)) - loss) < 1e-9
     idx = rng.choice(S.NPARAM, 200, replace=False)
     q = p.astype(np.float32).astype(np.float64)

@@ -17,6 +17,8 @@
 //     more (unions beyond kUnionCap are computed by the second-tier kernel);
 //   * work queue: (dilation, tile) items in decreasing predicted work (the
 //     network's per-tile candidate count, or the dilation's mean cost);
+//   * union capacity of the main kernel: 32, or 64 for dense inputs (more
+//     than 10 segments per column on average);
 //   * block shape: rows of 32 columns per block, chosen by the autotuner below
 //     and cached per context.
 // Then the closures are captured into one graph. vo_batch_run replays it and
@@ -58,8 +60,9 @@ struct DilPlan {
   int vol = 0;
   SlotVol in, out;
   const DeviceTables *T = nullptr;
-  float *zf = nullptr, *E = nullptr, *dom = nullptr;
-  float4 *segdom = nullptr;
+  float *zf = nullptr, *E = nullptr;
+  int4 *col = nullptr;
+  float4 *prec = nullptr;
   unsigned int *maxbits = nullptr;
   int2 *pairs = nullptr;
   int *mid_list = nullptr, *mid_count = nullptr;
@@ -170,7 +173,7 @@ int size_output(vo_ctx *ctx, vo_batch *b, DilPlan &d, double radius) {
       d.tile_work[t] = w >= 0 && w < 1e30 ? (float)w : 0.f;  // a diverged network must not break the sort
     }
     d.spill_base = (int)total;
-    d.spill_cap = (int)std::max<int64_t>(4096, total / 32);
+    d.spill_cap = (int)std::max<int64_t>(4096, total / 8);
     entries = total + d.spill_cap;
     if (entries > 2147483647LL) return set_error(ctx, VO_ERANGE, "batch: slot layout exceeds int32 offsets");
     rc = plan_alloc(ctx, b, &d.tcap, (size_t)d.tiles32);
@@ -205,7 +208,7 @@ BatchVol batch_vol(const DilPlan &d, int *ovf) {
   BatchVol v;
   const vo_grid &g = d.in.grid;
   v.A = FastArgs{g.nx, g.ny, d.T->host.W, d.in.beg, d.in.end, (const double *)d.in.z, d.zf, d.T->Hf, d.T->H,
-                 d.pairs, d.npairs, d.E, d.dom, d.segdom, d.T->dH, (d.T->host.Dy + 1) * d.T->host.W};
+                 d.pairs, d.npairs, d.E, d.col, d.prec};
   v.obeg = d.out.beg;
   v.oend = d.out.end;
   v.oz = d.out.z;
@@ -260,7 +263,7 @@ int sm_count() {
 // per column. Results are cached in the context per (log2 columns, radius
 // bucket, learned or not). Tuning launches write into the round's output
 // slots, which the real launch overwrites.
-int tune_shape(vo_ctx *ctx, vo_batch *b, const std::vector<DilPlan> &dils, const BatchVol *dvols,
+int tune_shape(vo_ctx *ctx, vo_batch *b, const std::vector<DilPlan> &dils, const BatchVol *dvols, int ka,
                int *fby_out) {
   int64_t cols = 0;
   double rmax = 0;
@@ -269,7 +272,7 @@ int tune_shape(vo_ctx *ctx, vo_batch *b, const std::vector<DilPlan> &dils, const
     rmax = std::max(rmax, b->radii[d.vol]);
   }
   const long long key = ((long long)std::ilogb((double)std::max<int64_t>(cols, 1)) << 16) |
-                        ((long long)(rmax / 8) << 1) | (ctx->sizer ? 1 : 0);
+                        ((long long)(rmax / 8) << 2) | (ka == 64 ? 2 : 0) | (ctx->sizer ? 1 : 0);
   for (const auto &kv : ctx->tune_cache)
     if (kv.first == key) {
       *fby_out = kv.second;
@@ -284,7 +287,7 @@ int tune_shape(vo_ctx *ctx, vo_batch *b, const std::vector<DilPlan> &dils, const
   size_t qcap = 0;
   for (int fby : kTuneShapes) {
     if (rc) break;
-    const int per_sm = fast_batched_blocks_per_sm(fby);
+    const int per_sm = fast_batched_blocks_per_sm(ka, fby);
     if (per_sm <= 0) continue;
     const std::vector<int2> full = build_queue(dils, fby);
     const size_t want = std::max<size_t>(512, full.size() / 16);
@@ -307,7 +310,7 @@ int tune_shape(vo_ctx *ctx, vo_batch *b, const std::vector<DilPlan> &dils, const
         cudaMemsetAsync(d.mid_count, 0, sizeof(int), ctx->stream);
       }
       cudaEventRecord(ctx->ev[2], ctx->stream);
-      fast_batched_launch(fby, grid, ctx->stream, dvols, dq, (int)sample.size(), dnext);
+      fast_batched_launch(ka, fby, grid, ctx->stream, dvols, dq, (int)sample.size(), dnext);
       cudaEventRecord(ctx->ev[3], ctx->stream);
       cudaError_t e = cudaStreamSynchronize(ctx->stream);
       if (e != cudaSuccess) {
@@ -342,22 +345,23 @@ int plan_dilation_round(vo_ctx *ctx, vo_batch *b, std::vector<DilPlan> &dils, bo
     d.npairs = (int)pairs.size();
     rc = plan_alloc(ctx, b, &d.zf, 2 * (size_t)std::max<int64_t>(d.in.entries, 1));
     if (!rc) rc = plan_alloc(ctx, b, &d.E, 1);
-    if (!rc) rc = plan_alloc(ctx, b, &d.dom, (size_t)4 * ncols);
-    if (!rc) rc = plan_alloc(ctx, b, &d.segdom, (size_t)std::max<int64_t>(d.in.entries, 1));
+    if (!rc) rc = plan_alloc(ctx, b, &d.col, (size_t)ncols);
+    if (!rc) rc = plan_alloc(ctx, b, &d.prec, pairs.size());
     if (!rc) rc = plan_alloc(ctx, b, &d.mid_list, (size_t)ncols);
     if (!rc) rc = plan_alloc(ctx, b, &d.mid_count, 1);
     if (!rc) rc = plan_alloc(ctx, b, &d.maxbits, 1);
     if (!rc) rc = plan_alloc(ctx, b, &d.pairs, pairs.size());
     if (rc) return rc;
     cudaMemcpyAsync(d.pairs, pairs.data(), sizeof(int2) * pairs.size(), cudaMemcpyHostToDevice, ctx->stream);
+    fast_pair_records(ctx->stream, d.pairs, d.npairs, *d.T, d.prec);  // static: built once, not replayed
     VO_CK(ctx, cudaStreamSynchronize(ctx->stream));
     const SlotVol in = d.in;
-    float *zf = d.zf, *E = d.E, *dom = d.dom;
-    float4 *segdom = d.segdom;
+    float *zf = d.zf, *E = d.E;
+    int4 *col = d.col;
     unsigned int *mb = d.maxbits;
     const float R = (float)b->radii[d.vol];
-    record(b, 3, [in, zf, E, mb, R, dom, segdom](cudaStream_t st) {
-      fast_prepare(st, in.grid.nx, in.grid.ny, in.beg, in.end, in.z, zf, mb, R, E, dom, segdom);
+    record(b, 3, [in, zf, E, mb, R, col](cudaStream_t st) {
+      fast_prepare(st, in.grid.nx, in.grid.ny, in.beg, in.end, in.z, zf, mb, R, E, col);
     });
     // candidates per column ~ 4 x pairs x mean segments of the input (no sizer)
     const double segs = d.in.cap > 0 && d.in.owns ? d.in.cap * 0.5 : (double)d.in.entries / std::max(ncols, 1);
@@ -378,9 +382,17 @@ int plan_dilation_round(vo_ctx *ctx, vo_batch *b, std::vector<DilPlan> &dils, bo
   if (rc) return rc;
   cudaMemcpyAsync(dvols, hv.data(), sizeof(BatchVol) * hv.size(), cudaMemcpyHostToDevice, ctx->stream);
   VO_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  // union capacity of the round: 64 when its inputs average more than 10 segments per column
+  double segs = 0, cols = 0;
+  for (const DilPlan &d : dils) {
+    const double nc = (double)d.in.grid.nx * d.in.grid.ny;
+    segs += d.in.owns ? 0.5 * d.in.cap * nc : (double)d.in.entries;
+    cols += nc;
+  }
+  const int ka = fast_union_cap(segs / std::max(cols, 1.0));
   int fby = 4;
   run_pending(ctx, b);  // tuning reads the dilation inputs
-  rc = tune_shape(ctx, b, dils, dvols, &fby);
+  rc = tune_shape(ctx, b, dils, dvols, ka, &fby);
   if (rc) return rc;
   const std::vector<int2> q = build_queue(dils, fby);
   int2 *dq = nullptr;
@@ -388,7 +400,7 @@ int plan_dilation_round(vo_ctx *ctx, vo_batch *b, std::vector<DilPlan> &dils, bo
   if (rc) return rc;
   cudaMemcpyAsync(dq, q.data(), sizeof(int2) * q.size(), cudaMemcpyHostToDevice, ctx->stream);
   VO_CK(ctx, cudaStreamSynchronize(ctx->stream));
-  const int per_sm = std::max(1, fast_batched_blocks_per_sm(fby));
+  const int per_sm = std::max(1, fast_batched_blocks_per_sm(ka, fby));
   const int grid = std::max(1, std::min<int>((int)q.size(), sms * per_sm));
   std::vector<int *> counters;  // reset before every replay
   for (DilPlan &d : dils) {
@@ -399,10 +411,11 @@ int plan_dilation_round(vo_ctx *ctx, vo_batch *b, std::vector<DilPlan> &dils, bo
   record(b, 2, [=](cudaStream_t st) {
     cudaMemsetAsync(dnext, 0, sizeof(int), st);
     for (int *s : counters) cudaMemsetAsync(s, 0, sizeof(int), st);
-    fast_batched_launch(fby, grid, st, dvols, dq, nq, dnext);
+    fast_batched_launch(ka, fby, grid, st, dvols, dq, nq, dnext);
     fast_batched_mid_launch(st, dvols, nv, gmid);
   });
   b->stats.tile_rows = fby;
+  b->stats.union_cap = ka;
   b->stats.tiles += nq;
   if (later_rounds) run_pending(ctx, b);
   return VO_OK;

@@ -21,11 +21,11 @@
 // endpoints are always recomputed in FP64 from their identities, so results
 // are bit-identical to the FP64 oracle.
 //
-// Dominance: a source segment whose candidate lies inside the candidate of
-// its container in the neighbouring source column one lattice step toward the
-// output column (H grows by at least dH over that step) is skipped; whole
-// source columns are skipped when all their segments are. Both bounds are
-// computed with directed rounding, so skipping never changes the union.
+// Dominance: a source column whose segments all lie in segments of its
+// neighbour one lattice step toward the output column, widened by at most the
+// growth dH of H over that step, adds nothing that neighbour's candidates do
+// not cover, and is skipped. Both bounds are computed with directed rounding,
+// so skipping never changes the union.
 //
 // Capacities: the main kernels keep kUnionCap (32) intervals per column;
 // columns that need more are re-run by the same code with kUnionCapMid (128)
@@ -36,6 +36,8 @@
 #include <cmath>
 #include <cstring>
 #include <vector>
+
+#include <cuda_fp16.h>
 
 #include "vo_internal.cuh"
 
@@ -86,6 +88,11 @@ __device__ __noinline__ bool ex_u_lt_u(const FastArgs &A, const UnionIds<KA> &U,
   return a < b;
 }
 
+// The FP16 in the low (lo != 0) or high half of v, as a float.
+__device__ __forceinline__ float half_lo_hi(unsigned v, int lo) {
+  return __half2float(__ushort_as_half((unsigned short)(lo ? (v & 0xffffu) : (v >> 16))));
+}
+
 // FP32 difference t = y - x decides x < y outside the guard band [-E, E].
 #define GUARD(t, E, exact) ((t) > (E) ? true : ((t) < -(E) ? false : (exact)))
 
@@ -100,40 +107,51 @@ __device__ __noinline__ bool ex_u_lt_u(const FastArgs &A, const UnionIds<KA> &U,
 template <int KA>
 __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv, int stride, UnionIds<KA> &U,
                            unsigned mask) {
-  const int ncols = A.nx * A.ny;
   int n = 0;
   bool overflow = false;
 #define SV(k) sv[(k) * stride]
-  for (int p = 0; p < A.npairs; ++p) {
-    const int2 ad = A.pairs[p];
-    const int a = ad.x, d = ad.y;
-    const float h = A.Hf[d * A.W + a];
-    const int da = d | (a << 8);
-    // growth of H over one step toward the output column (x step, y step)
-    const float dhx = A.dom ? A.dH[d * A.W + a] : -INFINITY;
-    const float dhy = A.dom ? A.dH[A.dHy + d * A.W + a] : -INFINITY;
-    int kb0, ke0, kb1, ke1, kb2, ke2, kb3, ke3;
-    // Source S: x + a if S & 1 (its neighbour toward the output is at x - 1,
-    // direction "x-"), else x - a ("x+"); likewise y with S & 2.
-#define SRC(S, KB, KE)                                                                                  \
-  {                                                                                                     \
-    const int xs = ((S) & 1) ? x + a : x - a;                                                           \
-    const int ys = ((S) & 2) ? y + d : y - d;                                                           \
-    bool ok = !(((S) & 1) && a == 0) && !(((S) & 2) && d == 0) && xs >= 0 && xs < A.nx && ys >= 0 &&    \
-              ys < A.ny;                                                                                \
-    const int c = ok ? xs + A.nx * ys : 0;                                                              \
-    if (ok && A.dom) {                                                                                  \
-      const float wx = A.dom[((S) & 1 ? 0 : ncols) + c];                                                \
-      const float wy = A.dom[((S) & 2 ? 2 * ncols : 3 * ncols) + c];                                    \
-      ok = !(wx <= dhx || wy <= dhy);                                                                   \
-    }                                                                                                   \
-    KB = ok ? A.beg[c] : 0;                                                                             \
-    KE = ok ? A.end[c] : 0;                                                                             \
+  // The records of pair p + 1 (its table entry and its four source columns')
+  // are loaded while pair p's candidates are merged.
+  // Source S: x + a if S & 1 (its neighbour toward the output is at x - 1,
+  // direction "x-"), else x - a ("x+"); likewise y with S & 2.
+#define LOAD_SOURCES(PR, R0, R1, R2, R3)                                                              \
+  {                                                                                                   \
+    const int ad_ = __float_as_int((PR).x), a_ = ad_ & 0xffff, d_ = ad_ >> 16;                        \
+    const bool xm = x - a_ >= 0, xp = a_ > 0 && x + a_ < A.nx;                                        \
+    const bool ym = y - d_ >= 0, yp = d_ > 0 && y + d_ < A.ny;                                        \
+    const int4 z4 = make_int4(0, 0, 0, 0);                                                           \
+    R0 = xm && ym ? A.col[(x - a_) + A.nx * (y - d_)] : z4;                                           \
+    R1 = xp && ym ? A.col[(x + a_) + A.nx * (y - d_)] : z4;                                           \
+    R2 = xm && yp ? A.col[(x - a_) + A.nx * (y + d_)] : z4;                                           \
+    R3 = xp && yp ? A.col[(x + a_) + A.nx * (y + d_)] : z4;                                           \
   }
-    SRC(0, kb0, ke0)
-    SRC(1, kb1, ke1)
-    SRC(2, kb2, ke2)
-    SRC(3, kb3, ke3)
+  float4 pr = A.prec[0];
+  int4 r0, r1, r2, r3;
+  LOAD_SOURCES(pr, r0, r1, r2, r3)
+  for (int p = 0; p < A.npairs; ++p) {
+    const float4 pc = pr;
+    const int4 c0 = r0, c1 = r1, c2 = r2, c3 = r3;
+    if (p + 1 < A.npairs) {
+      pr = A.prec[p + 1];
+      LOAD_SOURCES(pr, r0, r1, r2, r3)
+    }
+    const int ad = __float_as_int(pc.x), a = ad & 0xffff, d = ad >> 16;
+    const float h = pc.y;
+    const int da = d | (a << 8);
+    // growth of H over one step toward the output column (x step, y step);
+    // a source column dominated in either direction is skipped
+    const float dhx = pc.z, dhy = pc.w;
+#define SRC(S, C, KB, KE)                                                                             \
+  {                                                                                                   \
+    const bool dom = half_lo_hi((unsigned)(C).z, (S) & 1) <= dhx || half_lo_hi((unsigned)(C).w, (S) & 2) <= dhy; \
+    KB = dom ? 0 : (C).x;                                                                             \
+    KE = dom ? 0 : (C).y;                                                                             \
+  }
+    int kb0, ke0, kb1, ke1, kb2, ke2, kb3, ke3;
+    SRC(0, c0, kb0, ke0)
+    SRC(1, c1, kb1, ke1)
+    SRC(2, c2, kb2, ke2)
+    SRC(3, c3, kb3, ke3)
 #undef SRC
     const int total = (ke0 - kb0) + (ke1 - kb1) + (ke2 - kb2) + (ke3 - kb3);
     const int iters = __reduce_max_sync(mask, total);
@@ -149,16 +167,11 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
           cur = 0;
           if (n > 0) cv = SV(0);
         }
-        bool dominated = false;
-        if (A.segdom) {
-          const float4 w = A.segdom[k];
-          dominated = ((s & 1) ? w.x : w.y) <= dhx || ((s & 2) ? w.z : w.w) <= dhy;
-        }
-        const float2 zf = *reinterpret_cast<const float2 *>(A.zf + 2 * k);
-        const float lo = zf.x - h, hi = zf.y + h;
-        const int il = 2 * k, ih = 2 * k + 1;
-        ++k;
-        if (!dominated) {
+        {
+          const float2 zf = *reinterpret_cast<const float2 *>(A.zf + 2 * k);
+          const float lo = zf.x - h, hi = zf.y + h;
+          const int il = 2 * k, ih = 2 * k + 1;
+          ++k;
           // skip union intervals that end strictly below the candidate: U.hi[cur] < lo
           while (cur < n && GUARD(lo - cv.y, E, ex_u_lt_c(A, U, cur, true, il, da, false))) {
             ++cur;
@@ -237,6 +250,7 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
     }
   }
 #undef SV
+#undef LOAD_SOURCES
   return overflow ? -1 : n;
 }
 
@@ -248,21 +262,22 @@ __device__ __forceinline__ void write_union(const FastArgs &A, const UnionIds<KA
 }
 
 // One pass: the exact union of every output column goes to its fixed-capacity
-// staging slot (kKA intervals) with its count; columns that need more are
+// staging slot (KA intervals) with its count; columns that need more are
 // listed for the second tier. A compaction pass then packs the slots.
+template <int KA>
 __global__ void __launch_bounds__(kFB *kFBY) k_fast(FastArgs A, int32_t *counts, double2 *staging,
                                                     int *ovf_count, int *ovf_cols) {
-  __shared__ float2 sv[kKA * kFB * kFBY];
+  extern __shared__ float2 sv_dyn[];
   const int tid = threadIdx.x + kFB * threadIdx.y;
   const int x = blockIdx.x * kFB + threadIdx.x;
   const int y = blockIdx.y * kFBY + threadIdx.y;
   if (x >= A.nx || y >= A.ny) return;
   const int c = x + A.nx * y;
   const float E = *A.E;
-  UnionIds<kKA> U;
+  UnionIds<KA> U;
   const unsigned mask = __activemask();
-  const int n = fast_column<kKA>(A, E, x, y, sv + tid, kFB * kFBY, U, mask);
-  if (n > 0) write_union(A, U, n, staging + (size_t)c * kKA);
+  const int n = fast_column<KA>(A, E, x, y, sv_dyn + tid, kFB * kFBY, U, mask);
+  if (n > 0) write_union(A, U, n, staging + (size_t)c * KA);
   if (n < 0) {
     ovf_cols[atomicAdd(ovf_count, 1)] = c;
     counts[c] = 0;
@@ -271,15 +286,17 @@ __global__ void __launch_bounds__(kFB *kFBY) k_fast(FastArgs A, int32_t *counts,
   }
 }
 
-// Packs the staging slots of the columns that fit into the CSR output.
-__global__ void k_compact(int ncols, const int32_t *__restrict__ counts, const double2 *__restrict__ staging,
-                          const int32_t *__restrict__ ooffs, double2 *__restrict__ oz) {
+// Packs the staging slots (ka intervals each) of the columns that fit into
+// the CSR output.
+__global__ void k_compact(int ncols, int ka, const int32_t *__restrict__ counts,
+                          const double2 *__restrict__ staging, const int32_t *__restrict__ ooffs,
+                          double2 *__restrict__ oz) {
   // one warp per column, lanes over intervals
   const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (w >= ncols) return;
   const int n = ooffs[w + 1] - ooffs[w];
-  if (n > kKA) return;  // written by the second tier
-  for (int k = lane; k < n; k += 32) oz[ooffs[w] + k] = staging[(size_t)w * kKA + k];
+  if (n > ka) return;  // written by the second tier
+  for (int k = lane; k < n; k += 32) oz[ooffs[w] + k] = staging[(size_t)w * ka + k];
 }
 
 // Second tier over the columns listed by k_fast (grid-stride): the same
@@ -433,11 +450,11 @@ __global__ void k_dh_tables(int Dy, int W, const double *__restrict__ H, const i
 // every difference rounded up (so w bounds the exact value from above; +inf
 // outside the grid or without a neighbour segment). The scan stops after the
 // first neighbour segment starting above segment i: every later neighbour
-// segment gives a larger value.
-// Per segment: float4 (x-, x+, y-, y+); per column and direction: the max
-// over its segments (-inf for an empty column).
+// segment gives a larger value. The column's width per direction is the max
+// over its segments (-inf for an empty column), stored as FP16 rounded up in
+// the column record col[c] = (beg, end, x- | x+ << 16, y- | y+ << 16).
 __global__ void k_dominance(int nx, int ny, const int32_t *__restrict__ beg, const int32_t *__restrict__ end,
-                            const double2 *__restrict__ z, float *__restrict__ dom, float4 *__restrict__ segdom) {
+                            const double2 *__restrict__ z, int4 *__restrict__ col) {
   const int ncols = nx * ny;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncols) return;
@@ -451,10 +468,9 @@ __global__ void k_dominance(int nx, int ny, const int32_t *__restrict__ beg, con
     nb0[k] = in ? beg[cn] : 0;
     nb1[k] = in ? end[cn] : 0;
   }
-  float cmax[4] = {-INFINITY, -INFINITY, -INFINITY, -INFINITY};
+  double cmax[4] = {-INFINITY, -INFINITY, -INFINITY, -INFINITY};
   for (int i = k0; i < k1; ++i) {
     const double2 si = z[i];
-    float w[4];
     for (int k = 0; k < 4; ++k) {
       double best = INFINITY;
       for (int j = nb0[k]; j < nb1[k]; ++j) {
@@ -464,12 +480,21 @@ __global__ void k_dominance(int nx, int ny, const int32_t *__restrict__ beg, con
         best = m < best ? m : best;
         if (sj.x > si.y) break;
       }
-      w[k] = __double2float_ru(best);
-      cmax[k] = w[k] > cmax[k] ? w[k] : cmax[k];
+      cmax[k] = best > cmax[k] ? best : cmax[k];
     }
-    if (segdom) segdom[i] = make_float4(w[0], w[1], w[2], w[3]);
   }
-  for (int k = 0; k < 4; ++k) dom[(size_t)k * ncols + c] = cmax[k];
+  unsigned h[4];
+  for (int k = 0; k < 4; ++k) h[k] = __half_as_ushort(__float2half_ru(__double2float_ru(cmax[k])));
+  col[c] = make_int4(k0, k1, (int)(h[0] | (h[1] << 16)), (int)(h[2] | (h[3] << 16)));
+}
+
+// Pair records: (a | d << 16 as float bits, H in FP32, dH x step, dH y step).
+__global__ void k_pair_records(const int2 *__restrict__ pairs, int npairs, const float *__restrict__ Hf,
+                               const float *__restrict__ dH, int W, int dHy, float4 *__restrict__ prec) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npairs) return;
+  const int a = pairs[p].x, d = pairs[p].y;
+  prec[p] = make_float4(__int_as_float(a | (d << 16)), Hf[d * W + a], dH[d * W + a], dH[dHy + d * W + a]);
 }
 
 // ---------------------------------------------------------------- batches
@@ -501,8 +526,8 @@ __device__ __forceinline__ int place_union(const BatchVol &V, int x, int y, int 
 // dilation of a batch: blocks pull (dilation, tile) items from a queue ordered
 // by decreasing estimated work, so uneven volumes balance across the SMs.
 // Each column's union goes to its slot (place_union); a union of more than
-// kKA intervals is listed for k_fast_batched_mid.
-template <int FBY>
+// KA intervals is listed for k_fast_batched_mid.
+template <int KA, int FBY>
 __global__ void __launch_bounds__(kFB *FBY) k_fast_batched(const BatchVol *vols, const int2 *queue, int nq,
                                                            int *next) {
   extern __shared__ float2 sv_dyn[];
@@ -522,9 +547,9 @@ __global__ void __launch_bounds__(kFB *FBY) k_fast_batched(const BatchVol *vols,
     const int y = (q.y / tiles_x) * FBY + threadIdx.y;
     if (x < nx && y < ny) {
       const int c = x + nx * y;
-      UnionIds<kKA> U;
+      UnionIds<KA> U;
       const unsigned mask = __activemask();
-      int n = fast_column<kKA>(V.A, *V.A.E, x, y, sv_dyn + tid, kFB * FBY, U, mask);
+      int n = fast_column<KA>(V.A, *V.A.E, x, y, sv_dyn + tid, kFB * FBY, U, mask);
       int dst = 0;
       if (n < 0) {
         V.mid_list[atomicAdd(V.mid_count, 1)] = c;
@@ -599,8 +624,9 @@ int dilate_fast(vo_ctx *ctx, double R, const vo_volume *in, vo_volume **out, vo_
   if (rc) return rc;
   const Tables &h = T->host;
   const std::vector<int2> pairs = fast_pairs(h);
-  float *zf = nullptr, *dE = nullptr, *dom = nullptr;
-  float4 *segdom = nullptr;
+  float *zf = nullptr, *dE = nullptr;
+  int4 *col = nullptr;
+  float4 *prec = nullptr;
   unsigned int *dmax = nullptr;
   int2 *dpairs = nullptr;
   int32_t *counts = nullptr;
@@ -612,8 +638,8 @@ int dilate_fast(vo_ctx *ctx, double R, const vo_volume *in, vo_volume **out, vo_
   const int gbig = sms, gmid = sms * 16;
   rc = dalloc(ctx, &zf, (size_t)std::max<int64_t>(2 * in->nseg, 2));
   if (!rc) rc = dalloc(ctx, &dE, 1);
-  if (!rc) rc = dalloc(ctx, &dom, (size_t)4 * ncols);
-  if (!rc) rc = dalloc(ctx, &segdom, (size_t)std::max<int64_t>(in->nseg, 1));
+  if (!rc) rc = dalloc(ctx, &col, (size_t)ncols);
+  if (!rc) rc = dalloc(ctx, &prec, pairs.size());
   if (!rc) rc = dalloc(ctx, &dmax, 1);
   if (!rc) rc = dalloc(ctx, &dpairs, pairs.size());
   if (!rc) rc = dalloc(ctx, &counts, (size_t)ncols);
@@ -624,18 +650,29 @@ int dilate_fast(vo_ctx *ctx, double R, const vo_volume *in, vo_volume **out, vo_
     cudaMemcpyAsync(dpairs, pairs.data(), sizeof(int2) * pairs.size(), cudaMemcpyHostToDevice, ctx->stream);
     cudaMemsetAsync(ctx->d_flags, 0, 3 * sizeof(int), ctx->stream);  // [0] tier-2 list, [1] fatal, [2] FP64 list
     cudaEventRecord(ctx->ev[0], ctx->stream);
-    fast_prepare(ctx->stream, nx, ny, in->offs, in->offs + 1, in->z, zf, dmax, (float)R, dE, dom, segdom);
-    ctx->launches += 3;
+    fast_prepare(ctx->stream, nx, ny, in->offs, in->offs + 1, in->z, zf, dmax, (float)R, dE, col);
+    fast_pair_records(ctx->stream, dpairs, (int)pairs.size(), *T, prec);
+    ctx->launches += 4;
     cudaEventRecord(ctx->ev[1], ctx->stream);
   }
   FastArgs A{nx, ny, h.W, in->offs, in->offs + 1, (const double *)in->z, zf, T->Hf, T->H, dpairs,
-             (int)pairs.size(), dE, dom, segdom, T->dH, (h.Dy + 1) * h.W};
+             (int)pairs.size(), dE, col, prec};
   const dim3 blk(kFB, kFBY), grd((nx + kFB - 1) / kFB, (ny + kFBY - 1) / kFBY);
+  // dense volumes (more than 10 segments per column on average) keep 64-interval unions
+  const int ka = fast_union_cap((double)in->nseg / std::max(ncols, 1));
+  const size_t smem = sizeof(float2) * ka * kFB * kFBY;
   double2 *staging = nullptr;
-  if (!rc) rc = dalloc(ctx, &staging, (size_t)ncols * kKA);
+  if (!rc) rc = dalloc(ctx, &staging, (size_t)ncols * ka);
+  if (!rc && ka == 64 &&
+      cudaFuncSetAttribute(reinterpret_cast<const void *>(&k_fast<64>), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess)
+    rc = cuda_error(ctx, cudaGetLastError(), "k_fast shared memory");
   if (!rc) {
     cudaEventRecord(ctx->ev[4], ctx->stream);
-    k_fast<<<grd, blk, 0, ctx->stream>>>(A, counts, staging, ctx->d_flags, ovf_cols);
+    if (ka == 64)
+      k_fast<64><<<grd, blk, smem, ctx->stream>>>(A, counts, staging, ctx->d_flags, ovf_cols);
+    else
+      k_fast<32><<<grd, blk, smem, ctx->stream>>>(A, counts, staging, ctx->d_flags, ovf_cols);
     k_fast_mid<false><<<gmid, kMidThreads, 0, ctx->stream>>>(A, counts, nullptr, nullptr, ctx->d_flags, ovf_cols,
                                                                ctx->d_flags + 2, big_cols);
     k_fast_big<false><<<gbig, kBigThreads, 0, ctx->stream>>>(A, counts, nullptr, nullptr, ctx->d_flags + 2,
@@ -651,8 +688,8 @@ int dilate_fast(vo_ctx *ctx, double R, const vo_volume *in, vo_volume **out, vo_
   }
   if (!rc) {
     cudaEventRecord(ctx->ev[6], ctx->stream);
-    k_compact<<<(int)(((int64_t)ncols * 32 + 255) / 256), 256, 0, ctx->stream>>>(ncols, counts, staging, res->offs,
-                                                                                 res->z);
+    k_compact<<<(int)(((int64_t)ncols * 32 + 255) / 256), 256, 0, ctx->stream>>>(ncols, ka, counts, staging,
+                                                                                 res->offs, res->z);
     k_fast_mid<true><<<gmid, kMidThreads, 0, ctx->stream>>>(A, nullptr, res->offs, res->z, ctx->d_flags, ovf_cols,
                                                               nullptr, nullptr);
     k_fast_big<true><<<gbig, kBigThreads, 0, ctx->stream>>>(A, nullptr, res->offs, res->z, ctx->d_flags + 2,
@@ -683,8 +720,8 @@ int dilate_fast(vo_ctx *ctx, double R, const vo_volume *in, vo_volume **out, vo_
   }
   dfree(ctx, zf);
   dfree(ctx, dE);
-  dfree(ctx, dom);
-  dfree(ctx, segdom);
+  dfree(ctx, col);
+  dfree(ctx, prec);
   dfree(ctx, dmax);
   dfree(ctx, dpairs);
   dfree(ctx, counts);
@@ -712,12 +749,17 @@ std::vector<int2> fast_pairs(const Tables &h) {
 }
 
 void fast_prepare(cudaStream_t st, int nx, int ny, const int32_t *beg, const int32_t *end, const double2 *z,
-                  float *zf, unsigned int *maxbits, float R, float *E, float *dom, float4 *segdom) {
+                  float *zf, unsigned int *maxbits, float R, float *E, int4 *col) {
   const int ncols = nx * ny;
   cudaMemsetAsync(maxbits, 0, sizeof(unsigned int), st);
   k_to_f32_cols<<<(ncols + 255) / 256, 256, 0, st>>>(ncols, beg, end, (const double *)z, zf, maxbits);
   k_guard<<<1, 1, 0, st>>>(maxbits, R, E);
-  if (dom) k_dominance<<<(ncols + 127) / 128, 128, 0, st>>>(nx, ny, beg, end, z, dom, segdom);
+  k_dominance<<<(ncols + 127) / 128, 128, 0, st>>>(nx, ny, beg, end, z, col);
+}
+
+void fast_pair_records(cudaStream_t st, const int2 *pairs, int npairs, const DeviceTables &T, float4 *prec) {
+  const int W = T.host.W;
+  k_pair_records<<<(npairs + 127) / 128, 128, 0, st>>>(pairs, npairs, T.Hf, T.dH, W, (T.host.Dy + 1) * W, prec);
 }
 
 void launch_dh_tables(cudaStream_t st, int Dy, int W, const double *H, const int *Dx, float *dH) {
@@ -725,31 +767,51 @@ void launch_dh_tables(cudaStream_t st, int Dy, int W, const double *H, const int
   k_dh_tables<<<(n + 127) / 128, 128, 0, st>>>(Dy, W, H, Dx, dH);
 }
 
+int fast_union_cap(double mean_segments_per_column) { return mean_segments_per_column > 10.0 ? 64 : 32; }
+
 namespace {
-template <int FBY>
-void *batched_fn() {
-  return reinterpret_cast<void *>(&k_fast_batched<FBY>);
-}
+template <int KA>
 void *batched_kernel(int fby) {
   switch (fby) {
     case 1:
-      return batched_fn<1>();
+      return reinterpret_cast<void *>(&k_fast_batched<KA, 1>);
     case 2:
-      return batched_fn<2>();
+      return reinterpret_cast<void *>(&k_fast_batched<KA, 2>);
     case 4:
-      return batched_fn<4>();
+      return reinterpret_cast<void *>(&k_fast_batched<KA, 4>);
     case 8:
-      return batched_fn<8>();
+      return reinterpret_cast<void *>(&k_fast_batched<KA, 8>);
   }
   return nullptr;
 }
+void *batched_kernel(int ka, int fby) { return ka == 64 ? batched_kernel<64>(fby) : batched_kernel<32>(fby); }
+
+template <int KA>
+void launch_batched(int fby, int grid, size_t smem, cudaStream_t st, const BatchVol *vols, const int2 *queue, int nq,
+                    int *next) {
+  const dim3 blk(kFB, fby);
+  switch (fby) {
+    case 1:
+      k_fast_batched<KA, 1><<<grid, blk, smem, st>>>(vols, queue, nq, next);
+      break;
+    case 2:
+      k_fast_batched<KA, 2><<<grid, blk, smem, st>>>(vols, queue, nq, next);
+      break;
+    case 4:
+      k_fast_batched<KA, 4><<<grid, blk, smem, st>>>(vols, queue, nq, next);
+      break;
+    default:
+      k_fast_batched<KA, 8><<<grid, blk, smem, st>>>(vols, queue, nq, next);
+  }
+}
 }  // namespace
 
-int fast_batched_blocks_per_sm(int fby) {
-  void *f = batched_kernel(fby);
+int fast_batched_blocks_per_sm(int ka, int fby) {
+  void *f = batched_kernel(ka, fby);
   if (!f) return 0;
-  const size_t smem = sizeof(float2) * kKA * kFB * fby;
-  if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+  const size_t smem = sizeof(float2) * ka * kFB * fby;
+  if (smem > 227 * 1024 ||
+      cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
@@ -761,26 +823,14 @@ int fast_batched_blocks_per_sm(int fby) {
   return per_sm;
 }
 
-int fast_batched_launch(int fby, int grid, cudaStream_t st, const BatchVol *vols, const int2 *queue, int nq,
+int fast_batched_launch(int ka, int fby, int grid, cudaStream_t st, const BatchVol *vols, const int2 *queue, int nq,
                         int *next) {
-  const size_t smem = sizeof(float2) * kKA * kFB * fby;
-  const dim3 blk(kFB, fby);
-  switch (fby) {
-    case 1:
-      k_fast_batched<1><<<grid, blk, smem, st>>>(vols, queue, nq, next);
-      break;
-    case 2:
-      k_fast_batched<2><<<grid, blk, smem, st>>>(vols, queue, nq, next);
-      break;
-    case 4:
-      k_fast_batched<4><<<grid, blk, smem, st>>>(vols, queue, nq, next);
-      break;
-    case 8:
-      k_fast_batched<8><<<grid, blk, smem, st>>>(vols, queue, nq, next);
-      break;
-    default:
-      return VO_EINVAL;
-  }
+  if ((ka != 32 && ka != 64) || (fby != 1 && fby != 2 && fby != 4 && fby != 8)) return VO_EINVAL;
+  const size_t smem = sizeof(float2) * ka * kFB * fby;
+  if (ka == 64)
+    launch_batched<64>(fby, grid, smem, st, vols, queue, nq, next);
+  else
+    launch_batched<32>(fby, grid, smem, st, vols, queue, nq, next);
   return VO_OK;
 }
 

@@ -175,10 +175,11 @@ struct FastArgs {
   const int2 *pairs;    // (a, d) sorted by decreasing H
   int npairs;
   const float *E;       // guard band (device scalar)
-  const float *dom;       // [4][ncols] column dominance widths (fast_prepare), or nullptr
-  const float4 *segdom;   // per segment dominance widths (x-, x+, y-, y+), or nullptr
-  const float *dH;        // DeviceTables::dH
-  int dHy;                // offset of the y-step half of dH: (Dy+1) * W
+  // Column records (beg, end, dominance widths x- | x+ << 16, y- | y+ << 16 as
+  // FP16) and pair records (a | d << 16 as float bits, H in FP32, dH of an x
+  // step, dH of a y step), both built by the fast_* helpers below.
+  const int4 *col;
+  const float4 *prec;
 };
 
 // One dilation of a batch (device array element of the persistent kernel).
@@ -205,16 +206,21 @@ void launch_dh_tables(cudaStream_t st, int Dy, int W, const double *H, const int
 // (a, d) pairs with a <= Dx[d], sorted by decreasing H (the candidate order of
 // the FP32 kernels).
 std::vector<int2> fast_pairs(const Tables &h);
-// FP32 copies of the values of a slot volume, the guard band scalar, and (dom
-// not null) the dominance widths: per column and direction (x-, x+, y-, y+)
-// into dom[4][ncols], per segment into segdom (may be null).
+// FP32 copies of the values of a slot volume, the guard band scalar, and the
+// column records (ncols int4).
 void fast_prepare(cudaStream_t st, int nx, int ny, const int32_t *beg, const int32_t *end, const double2 *z,
-                  float *zf, unsigned int *maxbits, float R, float *E, float *dom, float4 *segdom);
-// Launch of the persistent kernel with `fby` rows of kFB columns per block
-// (fby in {1, 2, 4, 8}); blocks_per_sm is the occupancy for that shape.
-int fast_batched_launch(int fby, int grid, cudaStream_t st, const BatchVol *vols, const int2 *queue, int nq,
+                  float *zf, unsigned int *maxbits, float R, float *E, int4 *col);
+// Pair records (npairs float4) from the device tables of radius T.
+void fast_pair_records(cudaStream_t st, const int2 *pairs, int npairs, const DeviceTables &T, float4 *prec);
+// Union capacity (32 or 64) of the main FP32 kernels for inputs with the
+// given mean segment count per column.
+int fast_union_cap(double mean_segments_per_column);
+// Launch of the persistent kernel with union capacity ka (32 or 64) and `fby`
+// rows of kFastCols columns per block (fby in {1, 2, 4, 8});
+// fast_batched_blocks_per_sm is the occupancy of that shape (0: unusable).
+int fast_batched_launch(int ka, int fby, int grid, cudaStream_t st, const BatchVol *vols, const int2 *queue, int nq,
                         int *next);
-int fast_batched_blocks_per_sm(int fby);
+int fast_batched_blocks_per_sm(int ka, int fby);
 // Second tier of a batch round over the dilations vols[0..nv) (grid-stride).
 void fast_batched_mid_launch(cudaStream_t st, const BatchVol *vols, int nv, int grid);
 constexpr int kFastCols = 32;  // columns per block row

@@ -12,8 +12,8 @@
 //
 // Network: 16 inputs -> 64 ReLU -> 64 ReLU -> 4 outputs (3 used), weights in
 // BF16 for inference, FP32 master copies, FP32 accumulation everywhere;
-// trained on the GPU with the kernels below (mean squared error on log2
-// targets, Adam). Layout of the flat parameter vector: W1[16][64], b1[64],
+// trained on the GPU with the kernels below (squared error on log2 targets,
+// under-prediction of the max count weighted 4x; Adam). Layout of the flat parameter vector: W1[16][64], b1[64],
 // W2[64][64], b2[64], W3[64][4], b3[4] (row-major, [in][out]).
 #include <cuda_bf16.h>
 
@@ -201,8 +201,11 @@ __global__ void k_mlp_forward(const float *__restrict__ X, int n, const __nv_bfl
 }
 
 // Backward through the activations: dz2 = (dout W3^T) * [h2 > 0],
-// dz1 = (dz2 W2^T) * [h1 > 0], with dout = 2 (out - target) / (n * NUSED) on
-// the used outputs. Also accumulates the squared error.
+// dz1 = (dz2 W2^T) * [h1 > 0], with dout = 2 w (out - target) / (n * NUSED)
+// on the used outputs. The loss is the weighted squared error with w =
+// kUnderWeight where the max-count output is below its target (slots sized
+// too small cost spills and re-runs, too large only memory), else 1.
+constexpr float kUnderWeight = 4.f;
 __global__ void k_mlp_backward_act(const float *__restrict__ out, const float *__restrict__ tgt, int n,
                                    const __nv_bfloat16 *__restrict__ w, const float *__restrict__ h1s,
                                    const float *__restrict__ h2s, float *__restrict__ dout, float *__restrict__ dz2,
@@ -216,8 +219,9 @@ __global__ void k_mlp_backward_act(const float *__restrict__ out, const float *_
     float go[NO];
     for (int k = 0; k < NO; ++k) {
       const float e = k < NUSED ? out[(size_t)s * NO + k] - tgt[(size_t)s * NUSED + k] : 0.f;
-      l += e * e;
-      go[k] = 2.f * e / (float)(n * NUSED);
+      const float wgt = (k == 0 && e < 0.f) ? kUnderWeight : 1.f;
+      l += wgt * e * e;
+      go[k] = 2.f * wgt * e / (float)(n * NUSED);
       dout[(size_t)s * NO + k] = go[k];
     }
     float g2[NH];
