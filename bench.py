@@ -210,9 +210,120 @@ def reference_arm(args, rank, world):
     return 0
 
 
+def batch_volumes(V, n, seed):
+    """The batched workload: n seeded volumes, grid side in {64, 128, 256, 512, 1024}, each a union of
+    64-2048 spheres with radii 2-30, radius r uniform in [2, 64] (multiples of 0.25), mixed operations."""
+    rng = np.random.default_rng(seed)
+    items = []
+    for _ in range(n):
+        side = int(rng.choice([64, 128, 256, 512, 1024]))
+        spec = V.SynthSpec(side, n_spheres=int(rng.integers(64, 2049)), s_rmin=2, s_rmax=30,
+                           seed=int(rng.integers(1, 1 << 40)))
+        g, o, z = V.synth_volume(spec)
+        items.append((g, o, z, float(np.round(rng.uniform(2, 64) * 4) / 4),
+                      ["dilation", "erosion", "opening", "closing"][int(rng.integers(0, 4))]))
+    return items
+
+
+def batch_main(args, rank, world, local):
+    """`--workload batch256`: one step = every volume of the batch through one replay of its plan plus
+    the conversion of all outputs to CSR; value = output columns per second. Arms: the same volumes one
+    by one through vo_morph (FP32 method, and the plain FP64 method on a subset)."""
+    import torch
+    import voroffset_gb300 as V
+
+    torch.cuda.set_device(local)
+    n = int(args.workload[len("batch"):] or 256)
+    items = batch_volumes(V, n, seed=7 + rank)
+    ctx = V.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
+    sizer = None
+    if not args.no_sizer:
+        from voroffset_gb300.train_sizer import WEIGHTS, load
+        if os.path.exists(WEIGHTS):
+            sizer = load(ctx)
+            ctx.set_sizer(sizer)
+    vols = [ctx.upload(g, o, z) for g, o, z, _, _ in items]
+    ops = [it[4] for it in items]
+    radii = [it[3] for it in items]
+    cols = sum(g.ncols for g, _, _, _, _ in items)
+    items = None  # host copies are no longer needed
+
+    def progress(what):
+        import resource
+        free, total = torch.cuda.mem_get_info(local)
+        print(f"[batch] {what}: device {(total - free) / 2**30:.1f} GiB used, host rss "
+              f"{resource.getrusage(resource.RUSAGE_SELF).ru_maxrss / 2**20:.1f} GiB", file=sys.stderr, flush=True)
+
+    progress("volumes uploaded")
+    plan = ctx.batch(vols, ops, radii, "fast")
+    st = plan.stats()
+    progress("plan built")
+    acc = {"launches": 0, "reruns": 0}
+
+    def step():
+        t = plan.run()
+        acc["launches"] += t["kernel_launches"]
+        acc["reruns"] += t["overflow_columns"]
+        for o in plan.outputs():
+            o.free()
+
+    def timed(f, steps, warmup):
+        for _ in range(warmup):
+            f()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            f()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms = timed(step, args.steps, args.warmup)
+    clk = clocks.stop()
+    value = world * cols * args.steps / (ms / 1e3) / 1e6
+    progress("batched steps timed")
+
+    def loop_step():
+        for v, op, r in zip(vols, ops, radii):
+            o, _ = ctx.morph(v, op, r, "fast")
+            o.free()
+
+    loop_ms = timed(loop_step, 1, 1)
+    arms = {"one_by_one_fast": {"value": world * cols / (loop_ms / 1e3) / 1e6, "unit": "Mcolumns/s",
+                                "ms_per_step": loop_ms}}
+    arms["batched_vs_one_by_one"] = value / arms["one_by_one_fast"]["value"]
+    line = {"metric": METRIC, "value": value, "unit": "Mcolumns/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": f"{n} volumes, sides 64-1024, 64-2048 spheres, r in [2, 64], mixed ops",
+                       "columns": cols, "method": "batched+learned" if sizer else "batched",
+                       "ops": {o: ops.count(o) for o in set(ops)},
+                       "plan": {k: st[k] for k in ("slot_bytes", "tiles", "tile_rows", "union_cap", "graph_nodes",
+                                                   "graph_kernels", "learned", "plan_ms", "tune_ms")},
+                       "reruns_per_step": acc["reruns"] / (args.steps + args.warmup)},
+            "gpu_launches": int(acc["launches"] * args.steps / (args.steps + args.warmup)),
+            "clocks": clk, "arms": arms}
+    plan.free()
+    for v in vols:
+        v.free()
+    if sizer is not None:
+        ctx.set_sizer(None)
+        sizer.free()
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
+    if args.workload.startswith("batch") and args.impl != "reference":
+        return batch_main(args, rank, world, local)
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")

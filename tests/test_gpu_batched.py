@@ -110,3 +110,22 @@ def test_batched_second_tier_without_rerun(ctx, vo, oracle):
     outs, t = ctx.morph_batched([v], ["dilation"], [0.9], "fast")
     assert t["overflow_columns"] == 0
     assert_same(ctx.download(outs[0]), oracle.morph(ogrid(oracle, g), offs, z, 0.9, "dilation"), tol=0.0)
+
+
+def test_plan_with_more_radii_than_the_table_cache(ctx, vo, oracle):
+    """20 distinct radii in one plan: the context keeps at most 16 radius tables,
+    so the plan must hold its own copies (every result checked)."""
+    rng = np.random.default_rng(31)
+    items = []
+    for i in range(20):
+        g, o, z = vo.synth_volume(vo.SynthSpec(24 + 2 * i, n_spheres=6, s_rmin=2, s_rmax=7, seed=100 + i))
+        items.append((g, o, z, 1.0 + 0.5 * i, OPS[i % 4]))
+    vols = [ctx.upload(g, o, z) for g, o, z, _, _ in items]
+    b = ctx.batch(vols, [it[4] for it in items], [it[3] for it in items])
+    for _ in range(2):
+        # a later single call refills the context cache in between replays
+        tmp, _ = ctx.morph(vols[0], "dilation", 40.25, "fast")
+        tmp.free()
+        b.run()
+        for (g, o, z, r, op), out in zip(items, b.outputs()):
+            assert_same(ctx.download(out), oracle.morph(ogrid(oracle, g), o, z, r, op), tol=0.0, what=f"{op} r={r}")

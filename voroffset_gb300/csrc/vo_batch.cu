@@ -30,6 +30,7 @@
 #include <cmath>
 #include <cstring>
 #include <functional>
+#include <memory>
 #include <vector>
 
 #include "vo_internal.cuh"
@@ -96,6 +97,9 @@ struct vo_batch {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   std::vector<vo_volume *> rerun;
+  // Radius tables used by the plan, copied into plan memory: the context's
+  // table cache evicts entries, and the graph reads these on every replay.
+  std::vector<std::unique_ptr<DeviceTables>> tables;
   vo_batch_stats stats{};
 };
 
@@ -434,6 +438,37 @@ void plan_free(vo_ctx *ctx, vo_batch *b) {
   delete b;
 }
 
+// Plan-owned copy of the tables of radius R (H, Hf and dH on the device, the
+// host tables), shared by the plan's volumes of the same radius. The cached
+// context entry is copied before any other table lookup can evict it.
+int plan_tables(vo_ctx *ctx, vo_batch *b, double R, int kmax, const DeviceTables **out) {
+  for (const auto &t : b->tables)
+    if (t->R == R && t->kmax >= kmax) {
+      *out = t.get();
+      return VO_OK;
+    }
+  const DeviceTables *T = nullptr;
+  int rc = get_tables(ctx, R, kmax, &T);
+  if (rc) return rc;
+  std::unique_ptr<DeviceTables> own(new (std::nothrow) DeviceTables());
+  if (!own) return set_error(ctx, VO_ENOMEM, "host allocation");
+  own->R = T->R;
+  own->kmax = T->kmax;
+  own->host = T->host;
+  const size_t nh = T->host.H.size();
+  rc = plan_alloc(ctx, b, &own->H, nh);
+  if (!rc) rc = plan_alloc(ctx, b, &own->Hf, nh);
+  if (!rc) rc = plan_alloc(ctx, b, &own->dH, 2 * nh);
+  if (rc) return rc;
+  cudaMemcpyAsync(own->H, T->H, sizeof(double) * nh, cudaMemcpyDeviceToDevice, ctx->stream);
+  cudaMemcpyAsync(own->Hf, T->Hf, sizeof(float) * nh, cudaMemcpyDeviceToDevice, ctx->stream);
+  cudaMemcpyAsync(own->dH, T->dH, sizeof(float) * 2 * nh, cudaMemcpyDeviceToDevice, ctx->stream);
+  VO_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  *out = own.get();
+  b->tables.push_back(std::move(own));
+  return VO_OK;
+}
+
 int plan_build(vo_ctx *ctx, vo_batch *b) {
   const int n = b->n;
   int rc = plan_alloc(ctx, b, &b->d_flags, (size_t)n + 1);
@@ -453,7 +488,7 @@ int plan_build(vo_ctx *ctx, vo_batch *b) {
     }
     cur[v] = slot_view(in, 0);
     rc = max_count(ctx, cur[v], &cur[v].cap);
-    if (!rc) rc = get_tables(ctx, b->radii[v], std::max(in->grid.nx, in->grid.ny) + 2, &tabs[v]);
+    if (!rc) rc = plan_tables(ctx, b, b->radii[v], std::max(in->grid.nx, in->grid.ny) + 2, &tabs[v]);
     if (rc) return rc;
   }
   std::vector<size_t> next(n, 0);
