@@ -153,25 +153,28 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
     SRC(2, c2, kb2, ke2)
     SRC(3, c3, kb3, ke3)
 #undef SRC
-    const int total = (ke0 - kb0) + (ke1 - kb1) + (ke2 - kb2) + (ke3 - kb3);
+    // The pair's candidates as one sequence t = 0 .. total-1 over the four
+    // sources; the FP32 values of candidate t + 1 are loaded while candidate t
+    // is merged.
+    const int e0 = ke0 - kb0, e1 = e0 + (ke1 - kb1), e2 = e1 + (ke2 - kb2);
+    const int total = e2 + (ke3 - kb3);
+#define KOF(t) ((t) < e0 ? kb0 + (t) : (t) < e1 ? kb1 + ((t) - e0) : (t) < e2 ? kb2 + ((t) - e1) : kb3 + ((t) - e2))
     const int iters = __reduce_max_sync(mask, total);
-    int s = 0, k = kb0, kend = ke0;
     int cur = 0;
     float2 cv = n > 0 ? SV(0) : make_float2(0.f, 0.f);
+    float2 znext = total > 0 ? *reinterpret_cast<const float2 *>(A.zf + 2 * KOF(0)) : make_float2(0.f, 0.f);
     for (int it = 0; it < iters; ++it) {
       if (it < total && !overflow) {
-        while (k >= kend) {  // next non-empty source column: restart the cursor
-          ++s;
-          k = s == 1 ? kb1 : (s == 2 ? kb2 : kb3);
-          kend = s == 1 ? ke1 : (s == 2 ? ke2 : ke3);
+        const int k = KOF(it);
+        if (it == e0 || it == e1 || it == e2) {  // first candidate of a new source column: restart the cursor
           cur = 0;
           if (n > 0) cv = SV(0);
         }
+        const float2 zf = znext;
+        if (it + 1 < total) znext = *reinterpret_cast<const float2 *>(A.zf + 2 * KOF(it + 1));
         {
-          const float2 zf = *reinterpret_cast<const float2 *>(A.zf + 2 * k);
           const float lo = zf.x - h, hi = zf.y + h;
           const int il = 2 * k, ih = 2 * k + 1;
-          ++k;
           // skip union intervals that end strictly below the candidate: U.hi[cur] < lo
           while (cur < n && GUARD(lo - cv.y, E, ex_u_lt_c(A, U, cur, true, il, da, false))) {
             ++cur;
@@ -251,6 +254,7 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
   }
 #undef SV
 #undef LOAD_SOURCES
+#undef KOF
   return overflow ? -1 : n;
 }
 
