@@ -141,7 +141,7 @@ typedef struct {
   int32_t learned;      /* 1 when slots and queue came from a sizer */
   int32_t reruns;       /* volumes re-run by the last vo_batch_run */
   double plan_ms;       /* host time of vo_batch_create */
-  double tune_ms[4];    /* autotuner sample times for 1, 2, 4, 8 rows (0: cached / not run) */
+  double tune_ms[4];    /* autotuner sample times for 1, 2, 4, 8 rows at the largest union capacity tried (0: cached) */
 } vo_batch_stats;
 int vo_batch_create(vo_ctx *ctx, int n, const int *ops, const double *radii, int method,
                     const vo_volume *const *ins, vo_batch **out);

@@ -15,12 +15,12 @@
 //     (plus a margin, at most kUnionCapMid); without one, every column gets
 //     kUnionCap slots; either way a spill region takes the columns that need
 //     more (unions beyond kUnionCap are computed by the second-tier kernel);
-//   * work queue: (dilation, tile) items in decreasing predicted work (the
-//     network's per-tile candidate count, or the dilation's mean cost);
-//   * union capacity of the main kernel: 32, or 64 for dense inputs (more
-//     than 10 segments per column on average);
-//   * block shape: rows of 32 columns per block, chosen by the autotuner below
-//     and cached per context.
+//   * work queue: dilations in decreasing predicted total work (the network's
+//     per-tile candidate counts, or the mean cost per column), the tiles of
+//     each in raster order;
+//   * union capacity of the main kernel (24 or 32; 64 for dense inputs, more
+//     than 10 segments per column on average) and block shape (rows of 32
+//     columns per block), chosen by the autotuner below and cached per context.
 // Then the closures are captured into one graph. vo_batch_run replays it and
 // re-runs, through the single-volume path, every volume whose overflow flag
 // is set (a union larger than its slot with the spill region exhausted, or
@@ -229,29 +229,36 @@ BatchVol batch_vol(const DilPlan &d, int *ovf) {
   return v;
 }
 
-// Work queue for blocks of kFastCols x fby columns, in decreasing estimated work.
+// Work queue for blocks of kFastCols x fby columns: dilations in decreasing
+// estimated total work (longest first, for the balance of the persistent
+// grid), each dilation's tiles in raster order so that the tiles running at
+// the same time share their source columns in L1 / L2.
 std::vector<int2> build_queue(const std::vector<DilPlan> &dils, int fby) {
-  struct Item {
-    float w;
-    int2 q;
-  };
-  std::vector<Item> items;
+  std::vector<std::pair<double, int>> order;
   for (size_t i = 0; i < dils.size(); ++i) {
     const DilPlan &d = dils[i];
     const vo_grid &g = d.in.grid;
-    const int tx = (g.nx + kFastCols - 1) / kFastCols, ty = (g.ny + fby - 1) / fby;
-    for (int t = 0; t < tx * ty; ++t) {
-      float w = (float)d.cost;
-      if (!d.tile_work.empty()) {
-        const int x = (t % tx) * kFastCols, y = (t / tx) * fby;
-        w = d.tile_work[(x / kSizerTile) + d.tiles32_x * (y / kSizerTile)];
+    double w = 0;
+    if (!d.tile_work.empty()) {
+      for (int t = 0; t < d.tiles32; ++t) {
+        const int tx = t % d.tiles32_x, ty = t / d.tiles32_x;
+        w += (double)d.tile_work[t] * std::min(kSizerTile, g.nx - tx * kSizerTile) *
+             std::min(kSizerTile, g.ny - ty * kSizerTile);
       }
-      items.push_back(Item{w, make_int2((int)i, t)});
+    } else {
+      w = d.cost * g.nx * (double)g.ny;
     }
+    order.push_back({w, (int)i});
   }
-  std::stable_sort(items.begin(), items.end(), [](const Item &a, const Item &b) { return a.w > b.w; });
-  std::vector<int2> q(items.size());
-  for (size_t i = 0; i < items.size(); ++i) q[i] = items[i].q;
+  std::stable_sort(order.begin(), order.end(), [](const std::pair<double, int> &a, const std::pair<double, int> &b) {
+    return a.first > b.first;
+  });
+  std::vector<int2> q;
+  for (const auto &o : order) {
+    const vo_grid &g = dils[o.second].in.grid;
+    const int tiles = ((g.nx + kFastCols - 1) / kFastCols) * ((g.ny + fby - 1) / fby);
+    for (int t = 0; t < tiles; ++t) q.push_back(make_int2(o.second, t));
+  }
   return q;
 }
 
@@ -262,13 +269,14 @@ int sm_count() {
   return sms > 0 ? sms : 1;
 }
 
-// Autotuner: times every block shape on an evenly strided sample of the
-// round's queue (about 1/16 of it, at least 512 items) and keeps the fastest
-// per column. Results are cached in the context per (log2 columns, radius
-// bucket, learned or not). Tuning launches write into the round's output
-// slots, which the real launch overwrites.
-int tune_shape(vo_ctx *ctx, vo_batch *b, const std::vector<DilPlan> &dils, const BatchVol *dvols, int ka,
-               int *fby_out) {
+// Autotuner: times every (union capacity, block shape) on an evenly strided
+// sample of the round's queue (about 1/16 of it, at least 512 items), the
+// second tier included, and keeps the fastest per column. Results are cached
+// in the context per (log2 columns, radius bucket, dense or not, learned or
+// not). Tuning launches write into the round's output slots, which the real
+// launch overwrites.
+int tune_shape(vo_ctx *ctx, vo_batch *b, const std::vector<DilPlan> &dils, const BatchVol *dvols, int ka_hint,
+               int *ka_out, int *fby_out) {
   int64_t cols = 0;
   double rmax = 0;
   for (const DilPlan &d : dils) {
@@ -276,12 +284,16 @@ int tune_shape(vo_ctx *ctx, vo_batch *b, const std::vector<DilPlan> &dils, const
     rmax = std::max(rmax, b->radii[d.vol]);
   }
   const long long key = ((long long)std::ilogb((double)std::max<int64_t>(cols, 1)) << 16) |
-                        ((long long)(rmax / 8) << 2) | (ka == 64 ? 2 : 0) | (ctx->sizer ? 1 : 0);
+                        ((long long)(rmax / 8) << 2) | (ka_hint == 64 ? 2 : 0) | (ctx->sizer ? 1 : 0);
   for (const auto &kv : ctx->tune_cache)
     if (kv.first == key) {
-      *fby_out = kv.second;
+      *ka_out = kv.second >> 8;
+      *fby_out = kv.second & 255;
       return VO_OK;
     }
+  // union capacities to try: 64 for dense inputs, else 24 and 32
+  std::vector<int> kas = ka_hint == 64 ? std::vector<int>{64} : std::vector<int>{24, 32};
+  int best_ka = kas.back();
   const int sms = sm_count();
   int best = 4;
   double best_t = 1e300;
@@ -289,6 +301,8 @@ int tune_shape(vo_ctx *ctx, vo_batch *b, const std::vector<DilPlan> &dils, const
   int2 *dq = nullptr;
   int rc = dalloc(ctx, &dnext, 1);
   size_t qcap = 0;
+  const int gmid = sms * 16;
+  for (int ka : kas)
   for (int fby : kTuneShapes) {
     if (rc) break;
     const int per_sm = fast_batched_blocks_per_sm(ka, fby);
@@ -315,6 +329,7 @@ int tune_shape(vo_ctx *ctx, vo_batch *b, const std::vector<DilPlan> &dils, const
       }
       cudaEventRecord(ctx->ev[2], ctx->stream);
       fast_batched_launch(ka, fby, grid, ctx->stream, dvols, dq, (int)sample.size(), dnext);
+      fast_batched_mid_launch(ctx->stream, dvols, (int)dils.size(), gmid);  // unions beyond ka count too
       cudaEventRecord(ctx->ev[3], ctx->stream);
       cudaError_t e = cudaStreamSynchronize(ctx->stream);
       if (e != cudaSuccess) {
@@ -325,16 +340,18 @@ int tune_shape(vo_ctx *ctx, vo_batch *b, const std::vector<DilPlan> &dils, const
     }
     if (rc) break;
     const double per_col = ms / ((double)sample.size() * kFastCols * fby);
-    b->stats.tune_ms[fby == 1 ? 0 : fby == 2 ? 1 : fby == 4 ? 2 : 3] = ms;
+    if (ka == kas.back()) b->stats.tune_ms[fby == 1 ? 0 : fby == 2 ? 1 : fby == 4 ? 2 : 3] = ms;
     if (per_col < best_t) {
       best_t = per_col;
       best = fby;
+      best_ka = ka;
     }
   }
   dfree(ctx, dnext);
   dfree(ctx, dq);
   if (rc) return rc;
-  ctx->tune_cache.push_back({key, best});
+  ctx->tune_cache.push_back({key, (best_ka << 8) | best});
+  *ka_out = best_ka;
   *fby_out = best;
   return VO_OK;
 }
@@ -393,10 +410,9 @@ int plan_dilation_round(vo_ctx *ctx, vo_batch *b, std::vector<DilPlan> &dils, bo
     segs += d.in.owns ? 0.5 * d.in.cap * nc : (double)d.in.entries;
     cols += nc;
   }
-  const int ka = fast_union_cap(segs / std::max(cols, 1.0));
-  int fby = 4;
+  int ka = fast_union_cap(segs / std::max(cols, 1.0)), fby = 4;
   run_pending(ctx, b);  // tuning reads the dilation inputs
-  rc = tune_shape(ctx, b, dils, dvols, ka, &fby);
+  rc = tune_shape(ctx, b, dils, dvols, ka, &ka, &fby);
   if (rc) return rc;
   const std::vector<int2> q = build_queue(dils, fby);
   int2 *dq = nullptr;

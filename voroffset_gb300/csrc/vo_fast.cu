@@ -531,9 +531,10 @@ __device__ __forceinline__ int place_union(const BatchVol &V, int x, int y, int 
 // by decreasing estimated work, so uneven volumes balance across the SMs.
 // Each column's union goes to its slot (place_union); a union of more than
 // KA intervals is listed for k_fast_batched_mid.
+// (At most 64 registers per thread: 1024 / (kFB * FBY) blocks per SM.)
 template <int KA, int FBY>
-__global__ void __launch_bounds__(kFB *FBY) k_fast_batched(const BatchVol *vols, const int2 *queue, int nq,
-                                                           int *next) {
+__global__ void __launch_bounds__(kFB *FBY, 1024 / (kFB * FBY)) k_fast_batched(const BatchVol *vols,
+                                                                               const int2 *queue, int nq, int *next) {
   extern __shared__ float2 sv_dyn[];
   __shared__ int s_item;
   const int tid = threadIdx.x + kFB * threadIdx.y;
@@ -662,7 +663,7 @@ int dilate_fast(vo_ctx *ctx, double R, const vo_volume *in, vo_volume **out, vo_
   FastArgs A{nx, ny, h.W, in->offs, in->offs + 1, (const double *)in->z, zf, T->Hf, T->H, dpairs,
              (int)pairs.size(), dE, col, prec};
   const dim3 blk(kFB, kFBY), grd((nx + kFB - 1) / kFB, (ny + kFBY - 1) / kFBY);
-  // dense volumes (more than 10 segments per column on average) keep 64-interval unions
+  // union capacity from the input's mean segment count per column (24, 32 or 64)
   const int ka = fast_union_cap((double)in->nseg / std::max(ncols, 1));
   const size_t smem = sizeof(float2) * ka * kFB * kFBY;
   double2 *staging = nullptr;
@@ -675,8 +676,10 @@ int dilate_fast(vo_ctx *ctx, double R, const vo_volume *in, vo_volume **out, vo_
     cudaEventRecord(ctx->ev[4], ctx->stream);
     if (ka == 64)
       k_fast<64><<<grd, blk, smem, ctx->stream>>>(A, counts, staging, ctx->d_flags, ovf_cols);
-    else
+    else if (ka == 32)
       k_fast<32><<<grd, blk, smem, ctx->stream>>>(A, counts, staging, ctx->d_flags, ovf_cols);
+    else
+      k_fast<24><<<grd, blk, smem, ctx->stream>>>(A, counts, staging, ctx->d_flags, ovf_cols);
     k_fast_mid<false><<<gmid, kMidThreads, 0, ctx->stream>>>(A, counts, nullptr, nullptr, ctx->d_flags, ovf_cols,
                                                                ctx->d_flags + 2, big_cols);
     k_fast_big<false><<<gbig, kBigThreads, 0, ctx->stream>>>(A, counts, nullptr, nullptr, ctx->d_flags + 2,
@@ -771,7 +774,9 @@ void launch_dh_tables(cudaStream_t st, int Dy, int W, const double *H, const int
   k_dh_tables<<<(n + 127) / 128, 128, 0, st>>>(Dy, W, H, Dx, dH);
 }
 
-int fast_union_cap(double mean_segments_per_column) { return mean_segments_per_column > 10.0 ? 64 : 32; }
+int fast_union_cap(double mean_segments_per_column) {
+  return mean_segments_per_column > 10.0 ? 64 : mean_segments_per_column > 6.0 ? 32 : 24;
+}
 
 namespace {
 template <int KA>
@@ -788,7 +793,9 @@ void *batched_kernel(int fby) {
   }
   return nullptr;
 }
-void *batched_kernel(int ka, int fby) { return ka == 64 ? batched_kernel<64>(fby) : batched_kernel<32>(fby); }
+void *batched_kernel(int ka, int fby) {
+  return ka == 64 ? batched_kernel<64>(fby) : ka == 32 ? batched_kernel<32>(fby) : ka == 24 ? batched_kernel<24>(fby) : nullptr;
+}
 
 template <int KA>
 void launch_batched(int fby, int grid, size_t smem, cudaStream_t st, const BatchVol *vols, const int2 *queue, int nq,
@@ -829,12 +836,14 @@ int fast_batched_blocks_per_sm(int ka, int fby) {
 
 int fast_batched_launch(int ka, int fby, int grid, cudaStream_t st, const BatchVol *vols, const int2 *queue, int nq,
                         int *next) {
-  if ((ka != 32 && ka != 64) || (fby != 1 && fby != 2 && fby != 4 && fby != 8)) return VO_EINVAL;
+  if ((ka != 24 && ka != 32 && ka != 64) || (fby != 1 && fby != 2 && fby != 4 && fby != 8)) return VO_EINVAL;
   const size_t smem = sizeof(float2) * ka * kFB * fby;
   if (ka == 64)
     launch_batched<64>(fby, grid, smem, st, vols, queue, nq, next);
-  else
+  else if (ka == 32)
     launch_batched<32>(fby, grid, smem, st, vols, queue, nq, next);
+  else
+    launch_batched<24>(fby, grid, smem, st, vols, queue, nq, next);
   return VO_OK;
 }
 

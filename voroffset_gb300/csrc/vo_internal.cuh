@@ -212,10 +212,10 @@ void fast_prepare(cudaStream_t st, int nx, int ny, const int32_t *beg, const int
                   float *zf, unsigned int *maxbits, float R, float *E, int4 *col);
 // Pair records (npairs float4) from the device tables of radius T.
 void fast_pair_records(cudaStream_t st, const int2 *pairs, int npairs, const DeviceTables &T, float4 *prec);
-// Union capacity (32 or 64) of the main FP32 kernels for inputs with the
+// Union capacity (24, 32 or 64) of the main FP32 kernels for inputs with the
 // given mean segment count per column.
 int fast_union_cap(double mean_segments_per_column);
-// Launch of the persistent kernel with union capacity ka (32 or 64) and `fby`
+// Launch of the persistent kernel with union capacity ka (24, 32 or 64) and `fby`
 // rows of kFastCols columns per block (fby in {1, 2, 4, 8});
 // fast_batched_blocks_per_sm is the occupancy of that shape (0: unusable).
 int fast_batched_launch(int ka, int fby, int grid, cudaStream_t st, const BatchVol *vols, const int2 *queue, int nq,
