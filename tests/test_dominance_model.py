@@ -101,3 +101,78 @@ def test_pruned_union_equals_oracle(vo, oracle, R, seed):
         want = wz[2 * wo[c]:2 * wo[c + 1]].reshape(-1, 2)
         assert np.array_equal(np.array(got[c]).reshape(-1, 2), want), c
     assert kept < total  # the rule prunes something on these shapes
+
+
+LEVELS = [0.0, 1 / 16, 1 / 8, 1 / 4, 1 / 2, 1.0, 2.0, 4.0]
+
+
+def _level(dh):
+    """Largest level <= dh (-1: none), as the kernels quantise a pair's growth of H."""
+    lv = -1
+    for i, t in enumerate(LEVELS):
+        if t <= dh:
+            lv = i
+    return lv
+
+
+def _segment_widths(nx, ny, cols):
+    out = []
+    for c in range(nx * ny):
+        x, y = c % nx, c // nx
+        ws = []
+        for (a1, a2) in cols[c]:
+            w4 = []
+            for (ex, ey) in ((-1, 0), (1, 0), (0, -1), (0, 1)):
+                xn, yn = x + ex, y + ey
+                if not (0 <= xn < nx and 0 <= yn < ny):
+                    w4.append(np.inf)
+                    continue
+                w4.append(min([max(np.nextafter(b1 - a1, np.inf), np.nextafter(a2 - b2, np.inf))
+                               for (b1, b2) in cols[xn + nx * yn]] or [np.inf]))
+            ws.append(w4)
+        out.append(ws)
+    return out
+
+
+@pytest.mark.parametrize("R,seed", [(3.0, 2), (6.0, 4), (7.5, 9)])
+def test_segment_masks_by_level_equal_oracle(vo, oracle, R, seed):
+    """Per-segment pruning with widths compared at the quantised level of the
+    pair's growth of H (the kernels' dominance masks) keeps the union exact."""
+    g, offs, z = vo.synth_volume(vo.SynthSpec(20, n_spheres=12, s_rmin=2, s_rmax=7, n_cyl=3, seed=seed))
+    nx, ny = g.nx, g.ny
+    cols = [list(map(tuple, z[2 * offs[c]:2 * offs[c + 1]].reshape(-1, 2))) for c in range(g.ncols)]
+    Dy, Dx, H = _tables(R)
+    sw = _segment_widths(nx, ny, cols)
+    lx = {(d, a): _level(_down(H[(d, a - 1)] - H[(d, a)])) if a >= 1 else -1 for (d, a) in H}
+    ly = {(d, a): _level(_down(H[(d - 1, a)] - H[(d, a)])) if d >= 1 else -1 for (d, a) in H}
+    kept = total = 0
+    wo, wz = oracle.morph(ogrid(oracle, g), offs, z, R, "dilation")
+    for c in range(nx * ny):
+        x, y = c % nx, c // nx
+        cand = []
+        for (d, a), h in H.items():
+            for sx in ((1, -1) if a else (1,)):
+                for sy in ((1, -1) if d else (1,)):
+                    xs, ys = x + sx * a, y + sy * d
+                    if not (0 <= xs < nx and 0 <= ys < ny):
+                        continue
+                    s = xs + nx * ys
+                    for i, (z1, z2) in enumerate(cols[s]):
+                        total += 1
+                        w = sw[s][i]
+                        wx, wy = w[0 if sx > 0 else 1], w[2 if sy > 0 else 3]
+                        if (lx[(d, a)] >= 0 and wx <= LEVELS[lx[(d, a)]]) or \
+                           (ly[(d, a)] >= 0 and wy <= LEVELS[ly[(d, a)]]):
+                            continue
+                        kept += 1
+                        cand.append((z1 - h, z2 + h))
+        cand.sort()
+        u = []
+        for lo, hi in cand:
+            if u and lo <= u[-1][1]:
+                u[-1][1] = max(u[-1][1], hi)
+            else:
+                u.append([lo, hi])
+        want = wz[2 * wo[c]:2 * wo[c + 1]].reshape(-1, 2)
+        assert np.array_equal(np.array(u).reshape(-1, 2), want), c
+    assert kept < total

@@ -64,6 +64,7 @@ struct DilPlan {
   float *zf = nullptr, *E = nullptr;
   int4 *col = nullptr;
   float4 *prec = nullptr;
+  unsigned *dmask = nullptr;
   unsigned int *maxbits = nullptr;
   int2 *pairs = nullptr;
   int *mid_list = nullptr, *mid_count = nullptr;
@@ -212,7 +213,7 @@ BatchVol batch_vol(const DilPlan &d, int *ovf) {
   BatchVol v;
   const vo_grid &g = d.in.grid;
   v.A = FastArgs{g.nx, g.ny, d.T->host.W, d.in.beg, d.in.end, (const double *)d.in.z, d.zf, d.T->Hf, d.T->H,
-                 d.pairs, d.npairs, d.E, d.col, d.prec};
+                 d.pairs, d.npairs, d.E, d.col, d.prec, d.dmask};
   v.obeg = d.out.beg;
   v.oend = d.out.end;
   v.oz = d.out.z;
@@ -367,6 +368,7 @@ int plan_dilation_round(vo_ctx *ctx, vo_batch *b, std::vector<DilPlan> &dils, bo
     rc = plan_alloc(ctx, b, &d.zf, 2 * (size_t)std::max<int64_t>(d.in.entries, 1));
     if (!rc) rc = plan_alloc(ctx, b, &d.E, 1);
     if (!rc) rc = plan_alloc(ctx, b, &d.col, (size_t)ncols);
+    if (!rc) rc = plan_alloc(ctx, b, &d.dmask, (size_t)4 * kDomLevels * ncols);
     if (!rc) rc = plan_alloc(ctx, b, &d.prec, pairs.size());
     if (!rc) rc = plan_alloc(ctx, b, &d.mid_list, (size_t)ncols);
     if (!rc) rc = plan_alloc(ctx, b, &d.mid_count, 1);
@@ -379,10 +381,11 @@ int plan_dilation_round(vo_ctx *ctx, vo_batch *b, std::vector<DilPlan> &dils, bo
     const SlotVol in = d.in;
     float *zf = d.zf, *E = d.E;
     int4 *col = d.col;
+    unsigned *dmask = d.dmask;
     unsigned int *mb = d.maxbits;
     const float R = (float)b->radii[d.vol];
-    record(b, 3, [in, zf, E, mb, R, col](cudaStream_t st) {
-      fast_prepare(st, in.grid.nx, in.grid.ny, in.beg, in.end, in.z, zf, mb, R, E, col);
+    record(b, 3, [in, zf, E, mb, R, col, dmask](cudaStream_t st) {
+      fast_prepare(st, in.grid.nx, in.grid.ny, in.beg, in.end, in.z, zf, mb, R, E, col, dmask);
     });
     // candidates per column ~ 4 x pairs x mean segments of the input (no sizer)
     const double segs = d.in.cap > 0 && d.in.owns ? d.in.cap * 0.5 : (double)d.in.entries / std::max(ncols, 1);

@@ -93,6 +93,9 @@ __device__ __forceinline__ float half_lo_hi(unsigned v, int lo) {
   return __half2float(__ushort_as_half((unsigned short)(lo ? (v & 0xffffu) : (v >> 16))));
 }
 
+// Dominance level thresholds: 0, 1/16, 1/8, 1/4, 1/2, 1, 2, 4 (exact in FP32).
+__device__ __forceinline__ float dom_level(int l) { return l == 0 ? 0.f : ldexpf(1.f, l - 5); }
+
 // FP32 difference t = y - x decides x < y outside the guard band [-E, E].
 #define GUARD(t, E, exact) ((t) > (E) ? true : ((t) < -(E) ? false : (exact)))
 
@@ -110,68 +113,119 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
   int n = 0;
   bool overflow = false;
 #define SV(k) sv[(k) * stride]
-  // The records of pair p + 1 (its table entry and its four source columns')
-  // are loaded while pair p's candidates are merged.
+  // The records of pair p + 1 (its table entry, its four source columns'
+  // records and their segment dominance masks at the pair's levels) are
+  // loaded while pair p's candidates are merged.
   // Source S: x + a if S & 1 (its neighbour toward the output is at x - 1,
-  // direction "x-"), else x - a ("x+"); likewise y with S & 2.
-#define LOAD_SOURCES(PR, R0, R1, R2, R3)                                                              \
-  {                                                                                                   \
-    const int ad_ = __float_as_int((PR).x), a_ = ad_ & 0xffff, d_ = ad_ >> 16;                        \
-    const bool xm = x - a_ >= 0, xp = a_ > 0 && x + a_ < A.nx;                                        \
-    const bool ym = y - d_ >= 0, yp = d_ > 0 && y + d_ < A.ny;                                        \
-    const int4 z4 = make_int4(0, 0, 0, 0);                                                           \
-    R0 = xm && ym ? A.col[(x - a_) + A.nx * (y - d_)] : z4;                                           \
-    R1 = xp && ym ? A.col[(x + a_) + A.nx * (y - d_)] : z4;                                           \
-    R2 = xm && yp ? A.col[(x - a_) + A.nx * (y + d_)] : z4;                                           \
-    R3 = xp && yp ? A.col[(x + a_) + A.nx * (y + d_)] : z4;                                           \
+  // direction "x-" = 0), else x - a ("x+" = 1); likewise y with S & 2
+  // ("y-" = 2, "y+" = 3).
+  const int ncols = A.nx * A.ny;
+#define MASK(DIR, LV, C) ((LV) < kDomLevels ? A.dmask[((DIR) * kDomLevels + (LV)) * ncols + (C)] : 0u)
+#define LOAD_ONE(OK, XS, YS, S, R, MX, MY)                                                              \
+  {                                                                                                     \
+    const int c_ = (OK) ? (XS) + A.nx * (YS) : 0;                                                       \
+    R = (OK) ? A.col[c_] : make_int4(0, 0, 0, 0);                                                       \
+    MX = (OK) ? MASK((S) & 1 ? 0 : 1, lx_, c_) : 0u;                                                    \
+    MY = (OK) ? MASK((S) & 2 ? 2 : 3, ly_, c_) : 0u;                                                    \
+  }
+#define LOAD_SOURCES(PR)                                                                                \
+  {                                                                                                     \
+    const int ad_ = __float_as_int((PR).x), a_ = ad_ & 0xff, d_ = (ad_ >> 8) & 0xff;                    \
+    const int lx_ = (ad_ >> 16) & 0xf, ly_ = (ad_ >> 20) & 0xf;                                         \
+    const bool xm = x - a_ >= 0, xp = a_ > 0 && x + a_ < A.nx;                                          \
+    const bool ym = y - d_ >= 0, yp = d_ > 0 && y + d_ < A.ny;                                          \
+    LOAD_ONE(xm && ym, x - a_, y - d_, 0, r0, mx0, my0)                                                 \
+    LOAD_ONE(xp && ym, x + a_, y - d_, 1, r1, mx1, my1)                                                 \
+    LOAD_ONE(xm && yp, x - a_, y + d_, 2, r2, mx2, my2)                                                 \
+    LOAD_ONE(xp && yp, x + a_, y + d_, 3, r3, mx3, my3)                                                 \
   }
   float4 pr = A.prec[0];
   int4 r0, r1, r2, r3;
-  LOAD_SOURCES(pr, r0, r1, r2, r3)
+  unsigned mx0, my0, mx1, my1, mx2, my2, mx3, my3;
+  LOAD_SOURCES(pr)
   for (int p = 0; p < A.npairs; ++p) {
     const float4 pc = pr;
     const int4 c0 = r0, c1 = r1, c2 = r2, c3 = r3;
+    const unsigned d0 = mx0 | my0, d1 = mx1 | my1, d2 = mx2 | my2, d3 = mx3 | my3;
     if (p + 1 < A.npairs) {
       pr = A.prec[p + 1];
-      LOAD_SOURCES(pr, r0, r1, r2, r3)
+      LOAD_SOURCES(pr)
     }
-    const int ad = __float_as_int(pc.x), a = ad & 0xffff, d = ad >> 16;
+    const int ad = __float_as_int(pc.x), a = ad & 0xff, d = (ad >> 8) & 0xff;
     const float h = pc.y;
     const int da = d | (a << 8);
-    // growth of H over one step toward the output column (x step, y step);
-    // a source column dominated in either direction is skipped
+    // growth of H over one step toward the output column (x step, y step): a
+    // source column dominated in either direction is skipped whole; of the
+    // others (up to 32 segments), the segments dominated at the pair's levels
     const float dhx = pc.z, dhy = pc.w;
-#define SRC(S, C, KB, KE)                                                                             \
-  {                                                                                                   \
+    // Per source: [kb, ke) and the mask of its kept segments (bit j: segment
+    // kb + j); a source of more than 32 segments keeps all (m = 0, dense).
+#define SRC(S, C, DM, KB, KE, M)                                                                        \
+  {                                                                                                     \
     const bool dom = half_lo_hi((unsigned)(C).z, (S) & 1) <= dhx || half_lo_hi((unsigned)(C).w, (S) & 2) <= dhy; \
-    KB = dom ? 0 : (C).x;                                                                             \
-    KE = dom ? 0 : (C).y;                                                                             \
+    KB = dom ? 0 : (C).x;                                                                               \
+    KE = dom ? 0 : (C).y;                                                                               \
+    const int ns_ = KE - KB;                                                                            \
+    M = ns_ <= 32 ? ~(DM) & (ns_ == 32 ? 0xffffffffu : ((1u << ns_) - 1u)) : 0u;                        \
   }
     int kb0, ke0, kb1, ke1, kb2, ke2, kb3, ke3;
-    SRC(0, c0, kb0, ke0)
-    SRC(1, c1, kb1, ke1)
-    SRC(2, c2, kb2, ke2)
-    SRC(3, c3, kb3, ke3)
+    unsigned m0, m1, m2, m3;
+    SRC(0, c0, d0, kb0, ke0, m0)
+    SRC(1, c1, d1, kb1, ke1, m1)
+    SRC(2, c2, d2, kb2, ke2, m2)
+    SRC(3, c3, d3, kb3, ke3, m3)
 #undef SRC
-    // The pair's candidates as one sequence t = 0 .. total-1 over the four
-    // sources; the FP32 values of candidate t + 1 are loaded while candidate t
-    // is merged.
-    const int e0 = ke0 - kb0, e1 = e0 + (ke1 - kb1), e2 = e1 + (ke2 - kb2);
-    const int total = e2 + (ke3 - kb3);
-#define KOF(t) ((t) < e0 ? kb0 + (t) : (t) < e1 ? kb1 + ((t) - e0) : (t) < e2 ? kb2 + ((t) - e1) : kb3 + ((t) - e2))
+#define KEPT(KB, KE, M) ((KE) - (KB) > 32 ? (KE) - (KB) : __popc(M))
+    const int total = KEPT(kb0, ke0, m0) + KEPT(kb1, ke1, m1) + KEPT(kb2, ke2, m2) + KEPT(kb3, ke3, m3);
+#undef KEPT
     const int iters = __reduce_max_sync(mask, total);
-    int cur = 0;
-    float2 cv = n > 0 ? SV(0) : make_float2(0.f, 0.f);
-    float2 znext = total > 0 ? *reinterpret_cast<const float2 *>(A.zf + 2 * KOF(0)) : make_float2(0.f, 0.f);
+    // Walk state: source s, its remaining mask ms (sparse) or next index kc
+    // (dense); NEXT yields the next kept candidate (KN, SN), or KN = -1.
+    int s = -1, kc = 0, kend = 0, kbs = 0;
+    unsigned ms = 0;
+    bool dense = false;
+#define NEXT(KN, SN)                                                                                    \
+  {                                                                                                     \
+    KN = -1;                                                                                            \
+    for (;;) {                                                                                          \
+      if (s >= 0) {                                                                                     \
+        if (dense) {                                                                                    \
+          if (kc < kend) {                                                                              \
+            KN = kc++;                                                                                  \
+            break;                                                                                      \
+          }                                                                                             \
+        } else if (ms) {                                                                                \
+          KN = kbs + __ffs(ms) - 1;                                                                     \
+          ms &= ms - 1;                                                                                 \
+          break;                                                                                        \
+        }                                                                                               \
+      }                                                                                                 \
+      if (s >= 3) break;                                                                                \
+      ++s;                                                                                              \
+      kbs = s == 0 ? kb0 : s == 1 ? kb1 : s == 2 ? kb2 : kb3;                                           \
+      kend = s == 0 ? ke0 : s == 1 ? ke1 : s == 2 ? ke2 : ke3;                                          \
+      ms = s == 0 ? m0 : s == 1 ? m1 : s == 2 ? m2 : m3;                                                \
+      dense = kend - kbs > 32;                                                                          \
+      kc = kbs;                                                                                         \
+    }                                                                                                   \
+    SN = s;                                                                                             \
+  }
+    int cur = 0, cur_src = -1;
+    float2 cv = make_float2(0.f, 0.f);
+    int kn, sn;
+    NEXT(kn, sn)
+    float2 znext = kn >= 0 ? *reinterpret_cast<const float2 *>(A.zf + 2 * kn) : make_float2(0.f, 0.f);
     for (int it = 0; it < iters; ++it) {
       if (it < total && !overflow) {
-        const int k = KOF(it);
-        if (it == e0 || it == e1 || it == e2) {  // first candidate of a new source column: restart the cursor
+        const int k = kn, src = sn;
+        const float2 zf = znext;
+        NEXT(kn, sn)
+        if (kn >= 0) znext = *reinterpret_cast<const float2 *>(A.zf + 2 * kn);
+        if (src != cur_src) {  // first candidate of a new source column: restart the cursor
+          cur_src = src;
           cur = 0;
           if (n > 0) cv = SV(0);
         }
-        const float2 zf = znext;
-        if (it + 1 < total) znext = *reinterpret_cast<const float2 *>(A.zf + 2 * KOF(it + 1));
         {
           const float lo = zf.x - h, hi = zf.y + h;
           const int il = 2 * k, ih = 2 * k + 1;
@@ -254,7 +308,9 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
   }
 #undef SV
 #undef LOAD_SOURCES
-#undef KOF
+#undef LOAD_ONE
+#undef MASK
+#undef NEXT
   return overflow ? -1 : n;
 }
 
@@ -458,7 +514,7 @@ __global__ void k_dh_tables(int Dy, int W, const double *__restrict__ H, const i
 // over its segments (-inf for an empty column), stored as FP16 rounded up in
 // the column record col[c] = (beg, end, x- | x+ << 16, y- | y+ << 16).
 __global__ void k_dominance(int nx, int ny, const int32_t *__restrict__ beg, const int32_t *__restrict__ end,
-                            const double2 *__restrict__ z, int4 *__restrict__ col) {
+                            const double2 *__restrict__ z, int4 *__restrict__ col, unsigned *__restrict__ dmask) {
   const int ncols = nx * ny;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncols) return;
@@ -473,6 +529,10 @@ __global__ void k_dominance(int nx, int ny, const int32_t *__restrict__ beg, con
     nb1[k] = in ? end[cn] : 0;
   }
   double cmax[4] = {-INFINITY, -INFINITY, -INFINITY, -INFINITY};
+  unsigned bits[4][kDomLevels];
+  for (int k = 0; k < 4; ++k)
+    for (int l = 0; l < kDomLevels; ++l) bits[k][l] = 0u;
+  const bool masked = k1 - k0 <= 32;
   for (int i = k0; i < k1; ++i) {
     const double2 si = z[i];
     for (int k = 0; k < 4; ++k) {
@@ -485,20 +545,39 @@ __global__ void k_dominance(int nx, int ny, const int32_t *__restrict__ beg, con
         if (sj.x > si.y) break;
       }
       cmax[k] = best > cmax[k] ? best : cmax[k];
+      if (masked) {
+        const float w = __double2float_ru(best);
+        for (int l = 0; l < kDomLevels; ++l)
+          if (w <= dom_level(l)) bits[k][l] |= 1u << (i - k0);
+      }
     }
   }
+  if (dmask)
+    for (int k = 0; k < 4; ++k)
+      for (int l = 0; l < kDomLevels; ++l) dmask[(size_t)(k * kDomLevels + l) * ncols + c] = bits[k][l];
   unsigned h[4];
   for (int k = 0; k < 4; ++k) h[k] = __half_as_ushort(__float2half_ru(__double2float_ru(cmax[k])));
   col[c] = make_int4(k0, k1, (int)(h[0] | (h[1] << 16)), (int)(h[2] | (h[3] << 16)));
 }
 
-// Pair records: (a | d << 16 as float bits, H in FP32, dH x step, dH y step).
+// Largest dominance level whose threshold is <= dh (15: none).
+__device__ __forceinline__ int dom_level_of(float dh) {
+  int lv = 15;
+  for (int l = 0; l < kDomLevels; ++l)
+    if (dom_level(l) <= dh) lv = l;
+  return lv;
+}
+
+// Pair records: (a | d << 8 | x-step level << 16 | y-step level << 20 as
+// float bits, H in FP32, dH x step, dH y step).
 __global__ void k_pair_records(const int2 *__restrict__ pairs, int npairs, const float *__restrict__ Hf,
                                const float *__restrict__ dH, int W, int dHy, float4 *__restrict__ prec) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= npairs) return;
   const int a = pairs[p].x, d = pairs[p].y;
-  prec[p] = make_float4(__int_as_float(a | (d << 16)), Hf[d * W + a], dH[d * W + a], dH[dHy + d * W + a]);
+  const float dx = dH[d * W + a], dy = dH[dHy + d * W + a];
+  const int code = a | (d << 8) | (dom_level_of(dx) << 16) | (dom_level_of(dy) << 20);
+  prec[p] = make_float4(__int_as_float(code), Hf[d * W + a], dx, dy);
 }
 
 // ---------------------------------------------------------------- batches
@@ -531,9 +610,9 @@ __device__ __forceinline__ int place_union(const BatchVol &V, int x, int y, int 
 // by decreasing estimated work, so uneven volumes balance across the SMs.
 // Each column's union goes to its slot (place_union); a union of more than
 // KA intervals is listed for k_fast_batched_mid.
-// (At most 64 registers per thread: 1024 / (kFB * FBY) blocks per SM.)
+// (At most 85 registers per thread: 768 / (kFB * FBY) blocks per SM.)
 template <int KA, int FBY>
-__global__ void __launch_bounds__(kFB *FBY, 1024 / (kFB * FBY)) k_fast_batched(const BatchVol *vols,
+__global__ void __launch_bounds__(kFB *FBY, 768 / (kFB * FBY)) k_fast_batched(const BatchVol *vols,
                                                                                const int2 *queue, int nq, int *next) {
   extern __shared__ float2 sv_dyn[];
   __shared__ int s_item;
@@ -632,6 +711,7 @@ int dilate_fast(vo_ctx *ctx, double R, const vo_volume *in, vo_volume **out, vo_
   float *zf = nullptr, *dE = nullptr;
   int4 *col = nullptr;
   float4 *prec = nullptr;
+  unsigned *dmask = nullptr;
   unsigned int *dmax = nullptr;
   int2 *dpairs = nullptr;
   int32_t *counts = nullptr;
@@ -644,6 +724,7 @@ int dilate_fast(vo_ctx *ctx, double R, const vo_volume *in, vo_volume **out, vo_
   rc = dalloc(ctx, &zf, (size_t)std::max<int64_t>(2 * in->nseg, 2));
   if (!rc) rc = dalloc(ctx, &dE, 1);
   if (!rc) rc = dalloc(ctx, &col, (size_t)ncols);
+  if (!rc) rc = dalloc(ctx, &dmask, (size_t)4 * kDomLevels * ncols);
   if (!rc) rc = dalloc(ctx, &prec, pairs.size());
   if (!rc) rc = dalloc(ctx, &dmax, 1);
   if (!rc) rc = dalloc(ctx, &dpairs, pairs.size());
@@ -655,13 +736,13 @@ int dilate_fast(vo_ctx *ctx, double R, const vo_volume *in, vo_volume **out, vo_
     cudaMemcpyAsync(dpairs, pairs.data(), sizeof(int2) * pairs.size(), cudaMemcpyHostToDevice, ctx->stream);
     cudaMemsetAsync(ctx->d_flags, 0, 3 * sizeof(int), ctx->stream);  // [0] tier-2 list, [1] fatal, [2] FP64 list
     cudaEventRecord(ctx->ev[0], ctx->stream);
-    fast_prepare(ctx->stream, nx, ny, in->offs, in->offs + 1, in->z, zf, dmax, (float)R, dE, col);
+    fast_prepare(ctx->stream, nx, ny, in->offs, in->offs + 1, in->z, zf, dmax, (float)R, dE, col, dmask);
     fast_pair_records(ctx->stream, dpairs, (int)pairs.size(), *T, prec);
     ctx->launches += 4;
     cudaEventRecord(ctx->ev[1], ctx->stream);
   }
   FastArgs A{nx, ny, h.W, in->offs, in->offs + 1, (const double *)in->z, zf, T->Hf, T->H, dpairs,
-             (int)pairs.size(), dE, col, prec};
+             (int)pairs.size(), dE, col, prec, dmask};
   const dim3 blk(kFB, kFBY), grd((nx + kFB - 1) / kFB, (ny + kFBY - 1) / kFBY);
   // union capacity from the input's mean segment count per column (24, 32 or 64)
   const int ka = fast_union_cap((double)in->nseg / std::max(ncols, 1));
@@ -728,6 +809,7 @@ int dilate_fast(vo_ctx *ctx, double R, const vo_volume *in, vo_volume **out, vo_
   dfree(ctx, zf);
   dfree(ctx, dE);
   dfree(ctx, col);
+  dfree(ctx, dmask);
   dfree(ctx, prec);
   dfree(ctx, dmax);
   dfree(ctx, dpairs);
@@ -756,12 +838,12 @@ std::vector<int2> fast_pairs(const Tables &h) {
 }
 
 void fast_prepare(cudaStream_t st, int nx, int ny, const int32_t *beg, const int32_t *end, const double2 *z,
-                  float *zf, unsigned int *maxbits, float R, float *E, int4 *col) {
+                  float *zf, unsigned int *maxbits, float R, float *E, int4 *col, unsigned *dmask) {
   const int ncols = nx * ny;
   cudaMemsetAsync(maxbits, 0, sizeof(unsigned int), st);
   k_to_f32_cols<<<(ncols + 255) / 256, 256, 0, st>>>(ncols, beg, end, (const double *)z, zf, maxbits);
   k_guard<<<1, 1, 0, st>>>(maxbits, R, E);
-  k_dominance<<<(ncols + 127) / 128, 128, 0, st>>>(nx, ny, beg, end, z, col);
+  k_dominance<<<(ncols + 127) / 128, 128, 0, st>>>(nx, ny, beg, end, z, col, dmask);
 }
 
 void fast_pair_records(cudaStream_t st, const int2 *pairs, int npairs, const DeviceTables &T, float4 *prec) {

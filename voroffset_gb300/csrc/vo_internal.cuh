@@ -180,7 +180,12 @@ struct FastArgs {
   // step, dH of a y step), both built by the fast_* helpers below.
   const int4 *col;
   const float4 *prec;
+  // Segment dominance masks [4 directions][kDomLevels][ncols]: bit j of a
+  // column with at most 32 segments is set when its segment j lies in a
+  // neighbour segment widened by the level's threshold.
+  const unsigned *dmask;
 };
+constexpr int kDomLevels = 8;
 
 // One dilation of a batch (device array element of the persistent kernel).
 constexpr int kSizerTile = 32;  // side of a sizing tile (columns)
@@ -206,10 +211,10 @@ void launch_dh_tables(cudaStream_t st, int Dy, int W, const double *H, const int
 // (a, d) pairs with a <= Dx[d], sorted by decreasing H (the candidate order of
 // the FP32 kernels).
 std::vector<int2> fast_pairs(const Tables &h);
-// FP32 copies of the values of a slot volume, the guard band scalar, and the
-// column records (ncols int4).
+// FP32 copies of the values of a slot volume, the guard band scalar, the
+// column records (ncols int4) and the dominance masks (4 * kDomLevels * ncols).
 void fast_prepare(cudaStream_t st, int nx, int ny, const int32_t *beg, const int32_t *end, const double2 *z,
-                  float *zf, unsigned int *maxbits, float R, float *E, int4 *col);
+                  float *zf, unsigned int *maxbits, float R, float *E, int4 *col, unsigned *dmask);
 // Pair records (npairs float4) from the device tables of radius T.
 void fast_pair_records(cudaStream_t st, const int2 *pairs, int npairs, const DeviceTables &T, float4 *prec);
 // Union capacity (24, 32 or 64) of the main FP32 kernels for inputs with the
