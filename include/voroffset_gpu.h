@@ -135,7 +135,8 @@ typedef struct {
   int64_t slot_bytes;   /* output slot memory of the dilations */
   int32_t tiles;        /* work-queue items over all rounds */
   int32_t tile_rows;    /* rows of 32 columns per block chosen by the autotuner (last round) */
-  int32_t union_cap;    /* union intervals per column of the main kernel (last round): 32 or 64 */
+  int32_t union_cap;    /* union intervals per column of the main kernel (last round): 24, 32 or 64 */
+  int32_t persistent;   /* 1: one wave of blocks pulling queue items; 0: one block per item (last round) */
   int32_t graph_nodes;  /* nodes of the captured graph */
   int32_t graph_kernels;/* kernel launches per replay */
   int32_t learned;      /* 1 when slots and queue came from a sizer */

@@ -270,14 +270,15 @@ int sm_count() {
   return sms > 0 ? sms : 1;
 }
 
-// Autotuner: times every (union capacity, block shape) on an evenly strided
-// sample of the round's queue (about 1/16 of it, at least 512 items), the
-// second tier included, and keeps the fastest per column. Results are cached
-// in the context per (log2 columns, radius bucket, dense or not, learned or
-// not). Tuning launches write into the round's output slots, which the real
-// launch overwrites.
+// Autotuner: times every (union capacity, block shape, persistent or one
+// block per item) on a sample of the round's queue (four evenly spaced
+// contiguous runs, about 1/16 of it and at least 512 items), the second tier
+// included, and keeps the fastest per column. Results are cached in the
+// context per (log2 columns, radius bucket, dense or not, learned or not).
+// Tuning launches write into the round's output slots, which the real launch
+// overwrites.
 int tune_shape(vo_ctx *ctx, vo_batch *b, const std::vector<DilPlan> &dils, const BatchVol *dvols, int ka_hint,
-               int *ka_out, int *fby_out) {
+               int *ka_out, int *fby_out, int *persistent_out) {
   int64_t cols = 0;
   double rmax = 0;
   for (const DilPlan &d : dils) {
@@ -288,13 +289,14 @@ int tune_shape(vo_ctx *ctx, vo_batch *b, const std::vector<DilPlan> &dils, const
                         ((long long)(rmax / 8) << 2) | (ka_hint == 64 ? 2 : 0) | (ctx->sizer ? 1 : 0);
   for (const auto &kv : ctx->tune_cache)
     if (kv.first == key) {
-      *ka_out = kv.second >> 8;
+      *ka_out = (kv.second >> 8) & 255;
       *fby_out = kv.second & 255;
+      *persistent_out = (kv.second >> 16) & 1;
       return VO_OK;
     }
   // union capacities to try: 64 for dense inputs, else 24 and 32
   std::vector<int> kas = ka_hint == 64 ? std::vector<int>{64} : std::vector<int>{24, 32};
-  int best_ka = kas.back();
+  int best_ka = kas.back(), best_pers = 1;
   const int sms = sm_count();
   int best = 4;
   double best_t = 1e300;
@@ -304,15 +306,21 @@ int tune_shape(vo_ctx *ctx, vo_batch *b, const std::vector<DilPlan> &dils, const
   size_t qcap = 0;
   const int gmid = sms * 16;
   for (int ka : kas)
-  for (int fby : kTuneShapes) {
+  for (int fby : kTuneShapes)
+  for (int pers = 1; pers >= 0; --pers) {
     if (rc) break;
     const int per_sm = fast_batched_blocks_per_sm(ka, fby);
     if (per_sm <= 0) continue;
+    // four contiguous runs of the queue, evenly spaced: neighbouring tiles run
+    // together as in the real launch, so the sample sees its cache reuse
     const std::vector<int2> full = build_queue(dils, fby);
-    const size_t want = std::max<size_t>(512, full.size() / 16);
-    const size_t stride = std::max<size_t>(1, full.size() / want);
+    const size_t want = std::min(full.size(), std::max<size_t>(512, full.size() / 16));
     std::vector<int2> sample;
-    for (size_t i = 0; i < full.size(); i += stride) sample.push_back(full[i]);
+    for (int r = 0; r < 4; ++r) {
+      const size_t len = want / 4 + (r < (int)(want % 4) ? 1 : 0);
+      const size_t at = std::min(full.size() - len, (full.size() * (2 * r + 1)) / 8);
+      sample.insert(sample.end(), full.begin() + at, full.begin() + at + len);
+    }
     if (sample.size() > qcap) {
       dfree(ctx, dq);
       qcap = sample.size();
@@ -320,7 +328,8 @@ int tune_shape(vo_ctx *ctx, vo_batch *b, const std::vector<DilPlan> &dils, const
       if (rc) break;
     }
     cudaMemcpyAsync(dq, sample.data(), sizeof(int2) * sample.size(), cudaMemcpyHostToDevice, ctx->stream);
-    const int grid = std::max(1, std::min<int>((int)sample.size(), sms * per_sm));
+    // persistent: one wave of blocks pulling items; otherwise one block per item
+    const int grid = pers ? std::max(1, std::min<int>((int)sample.size(), sms * per_sm)) : (int)sample.size();
     float ms = 0;
     for (int rep = 0; rep < 2; ++rep) {  // the first run warms caches and clocks
       cudaMemsetAsync(dnext, 0, sizeof(int), ctx->stream);
@@ -341,19 +350,21 @@ int tune_shape(vo_ctx *ctx, vo_batch *b, const std::vector<DilPlan> &dils, const
     }
     if (rc) break;
     const double per_col = ms / ((double)sample.size() * kFastCols * fby);
-    if (ka == kas.back()) b->stats.tune_ms[fby == 1 ? 0 : fby == 2 ? 1 : fby == 4 ? 2 : 3] = ms;
+    if (ka == kas.back() && pers) b->stats.tune_ms[fby == 1 ? 0 : fby == 2 ? 1 : fby == 4 ? 2 : 3] = ms;
     if (per_col < best_t) {
       best_t = per_col;
       best = fby;
       best_ka = ka;
+      best_pers = pers;
     }
   }
   dfree(ctx, dnext);
   dfree(ctx, dq);
   if (rc) return rc;
-  ctx->tune_cache.push_back({key, (best_ka << 8) | best});
+  ctx->tune_cache.push_back({key, (best_pers << 16) | (best_ka << 8) | best});
   *ka_out = best_ka;
   *fby_out = best;
+  *persistent_out = best_pers;
   return VO_OK;
 }
 
@@ -413,9 +424,9 @@ int plan_dilation_round(vo_ctx *ctx, vo_batch *b, std::vector<DilPlan> &dils, bo
     segs += d.in.owns ? 0.5 * d.in.cap * nc : (double)d.in.entries;
     cols += nc;
   }
-  int ka = fast_union_cap(segs / std::max(cols, 1.0)), fby = 4;
+  int ka = fast_union_cap(segs / std::max(cols, 1.0)), fby = 4, persistent = 1;
   run_pending(ctx, b);  // tuning reads the dilation inputs
-  rc = tune_shape(ctx, b, dils, dvols, ka, &ka, &fby);
+  rc = tune_shape(ctx, b, dils, dvols, ka, &ka, &fby, &persistent);
   if (rc) return rc;
   const std::vector<int2> q = build_queue(dils, fby);
   int2 *dq = nullptr;
@@ -424,7 +435,7 @@ int plan_dilation_round(vo_ctx *ctx, vo_batch *b, std::vector<DilPlan> &dils, bo
   cudaMemcpyAsync(dq, q.data(), sizeof(int2) * q.size(), cudaMemcpyHostToDevice, ctx->stream);
   VO_CK(ctx, cudaStreamSynchronize(ctx->stream));
   const int per_sm = std::max(1, fast_batched_blocks_per_sm(ka, fby));
-  const int grid = std::max(1, std::min<int>((int)q.size(), sms * per_sm));
+  const int grid = persistent ? std::max(1, std::min<int>((int)q.size(), sms * per_sm)) : std::max(1, (int)q.size());
   std::vector<int *> counters;  // reset before every replay
   for (DilPlan &d : dils) {
     counters.push_back(d.spill_used);
@@ -439,6 +450,7 @@ int plan_dilation_round(vo_ctx *ctx, vo_batch *b, std::vector<DilPlan> &dils, bo
   });
   b->stats.tile_rows = fby;
   b->stats.union_cap = ka;
+  b->stats.persistent = persistent;
   b->stats.tiles += nq;
   if (later_rounds) run_pending(ctx, b);
   return VO_OK;

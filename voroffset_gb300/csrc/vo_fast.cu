@@ -582,6 +582,8 @@ __global__ void k_pair_records(const int2 *__restrict__ pairs, int npairs, const
 
 // ---------------------------------------------------------------- batches
 
+static_assert(sizeof(BatchVol) % sizeof(int) == 0, "BatchVol is copied as ints");
+
 // Output slot of column (x, y) of a batch dilation for an n-interval union:
 // the column's own slot when its tile capacity allows, else spill space, else
 // -1 (the dilation's overflow flag is then set).
@@ -616,15 +618,22 @@ __global__ void __launch_bounds__(kFB *FBY, 768 / (kFB * FBY)) k_fast_batched(co
                                                                                const int2 *queue, int nq, int *next) {
   extern __shared__ float2 sv_dyn[];
   __shared__ int s_item;
+  __shared__ BatchVol s_vol;  // the item's arguments, read by every thread in the hot loop
   const int tid = threadIdx.x + kFB * threadIdx.y;
+  int cur_vol = -1;
   for (;;) {
     if (tid == 0) s_item = atomicAdd(next, 1);
     __syncthreads();
     const int item = s_item;
-    __syncthreads();
     if (item >= nq) return;
     const int2 q = queue[item];
-    const BatchVol &V = vols[q.x];
+    if (q.x != cur_vol) {
+      for (int i = tid; i < (int)(sizeof(BatchVol) / sizeof(int)); i += kFB * FBY)
+        reinterpret_cast<int *>(&s_vol)[i] = reinterpret_cast<const int *>(&vols[q.x])[i];
+      cur_vol = q.x;
+    }
+    __syncthreads();
+    const BatchVol &V = s_vol;
     const int nx = V.A.nx, ny = V.A.ny;
     const int tiles_x = (nx + kFB - 1) / kFB;
     const int x = (q.y % tiles_x) * kFB + threadIdx.x;
