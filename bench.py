@@ -247,6 +247,7 @@ def batch_main(args, rank, world, local):
     ops = [it[4] for it in items]
     radii = [it[3] for it in items]
     cols = sum(g.ncols for g, _, _, _, _ in items)
+    meta = [(g.nx, op, r) for g, _, _, r, op in items]
     items = None  # host copies are no longer needed
 
     def progress(what):
@@ -296,10 +297,17 @@ def batch_main(args, rank, world, local):
     arms = {"one_by_one_fast": {"value": world * cols / (loop_ms / 1e3) / 1e6, "unit": "Mcolumns/s",
                                 "ms_per_step": loop_ms}}
     arms["batched_vs_one_by_one"] = value / arms["one_by_one_fast"]["value"]
+    st_run = plan.stats()
+    rerun = None
+    if st_run["rerun_first"] >= 0:
+        side, op, r = meta[st_run["rerun_first"]]
+        rerun = {"volumes": st_run["reruns"], "first": {"side": side, "op": op, "radius": r},
+                 "cause": st_run["rerun_cause"]}
     line = {"metric": METRIC, "value": value, "unit": "Mcolumns/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
             "config": {"workload": f"{n} volumes, sides 64-1024, 64-2048 spheres, r in [2, 64], mixed ops",
+                       "rerun": rerun,
                        "columns": cols, "method": "batched+learned" if sizer else "batched",
                        "ops": {o: ops.count(o) for o in set(ops)},
                        "plan": {k: st[k] for k in ("slot_bytes", "tiles", "tile_rows", "union_cap", "persistent", "graph_nodes",

@@ -170,7 +170,7 @@ int size_output(vo_ctx *ctx, vo_batch *b, DilPlan &d, double radius) {
       const int cols = std::min(kSizerTile, g.nx - tx * kSizerTile) * std::min(kSizerTile, g.ny - ty * kSizerTile);
       // predicted max segments per column, with a margin against the error of a log2 estimate
       const double mx = std::exp2((double)hp[(size_t)t * 4]) - 1.0;
-      const int c = (int)std::min<double>(kUnionCapMid, std::max(1.0, std::ceil(mx * 1.25 + 2.0)));
+      const int c = (int)std::min<double>(kUnionCapMid, std::max(1.0, std::ceil(mx * 1.5 + 2.0)));
       cap[t] = c;
       off[t] = (int32_t)total;
       total += (int64_t)c * cols;
@@ -178,7 +178,7 @@ int size_output(vo_ctx *ctx, vo_batch *b, DilPlan &d, double radius) {
       d.tile_work[t] = w >= 0 && w < 1e30 ? (float)w : 0.f;  // a diverged network must not break the sort
     }
     d.spill_base = (int)total;
-    d.spill_cap = (int)std::max<int64_t>(4096, total / 8);
+    d.spill_cap = (int)std::max<int64_t>(4096, total / 4);
     entries = total + d.spill_cap;
     if (entries > 2147483647LL) return set_error(ctx, VO_ERANGE, "batch: slot layout exceeds int32 offsets");
     rc = plan_alloc(ctx, b, &d.tcap, (size_t)d.tiles32);
@@ -274,18 +274,19 @@ int sm_count() {
 // block per item) on a sample of the round's queue (four evenly spaced
 // contiguous runs, about 1/16 of it and at least 512 items), the second tier
 // included, and keeps the fastest per column. Results are cached in the
-// context per (log2 columns, radius bucket, dense or not, learned or not).
+// context per (one dilation or several, log2 columns, radius bucket, dense or
+// not, learned or not).
 // Tuning launches write into the round's output slots, which the real launch
 // overwrites.
-int tune_shape(vo_ctx *ctx, vo_batch *b, const std::vector<DilPlan> &dils, const BatchVol *dvols, int ka_hint,
-               int *ka_out, int *fby_out, int *persistent_out) {
+int tune_shape(vo_ctx *ctx, vo_batch *b, const std::vector<DilPlan> &dils, const BatchVol *dvols,
+               const FastArgs *single, int ka_hint, int *ka_out, int *fby_out, int *persistent_out) {
   int64_t cols = 0;
   double rmax = 0;
   for (const DilPlan &d : dils) {
     cols += (int64_t)d.in.grid.nx * d.in.grid.ny;
     rmax = std::max(rmax, b->radii[d.vol]);
   }
-  const long long key = ((long long)std::ilogb((double)std::max<int64_t>(cols, 1)) << 16) |
+  const long long key = (single ? 1LL << 40 : 0) | ((long long)std::ilogb((double)std::max<int64_t>(cols, 1)) << 16) |
                         ((long long)(rmax / 8) << 2) | (ka_hint == 64 ? 2 : 0) | (ctx->sizer ? 1 : 0);
   for (const auto &kv : ctx->tune_cache)
     if (kv.first == key) {
@@ -309,7 +310,7 @@ int tune_shape(vo_ctx *ctx, vo_batch *b, const std::vector<DilPlan> &dils, const
   for (int fby : kTuneShapes)
   for (int pers = 1; pers >= 0; --pers) {
     if (rc) break;
-    const int per_sm = fast_batched_blocks_per_sm(ka, fby);
+    const int per_sm = fast_batched_blocks_per_sm(ka, fby, single != nullptr);
     if (per_sm <= 0) continue;
     // four contiguous runs of the queue, evenly spaced: neighbouring tiles run
     // together as in the real launch, so the sample sees its cache reuse
@@ -338,7 +339,7 @@ int tune_shape(vo_ctx *ctx, vo_batch *b, const std::vector<DilPlan> &dils, const
         cudaMemsetAsync(d.mid_count, 0, sizeof(int), ctx->stream);
       }
       cudaEventRecord(ctx->ev[2], ctx->stream);
-      fast_batched_launch(ka, fby, grid, ctx->stream, dvols, dq, (int)sample.size(), dnext);
+      fast_batched_launch(ka, fby, grid, ctx->stream, dvols, dq, (int)sample.size(), dnext, single);
       fast_batched_mid_launch(ctx->stream, dvols, (int)dils.size(), gmid);  // unions beyond ka count too
       cudaEventRecord(ctx->ev[3], ctx->stream);
       cudaError_t e = cudaStreamSynchronize(ctx->stream);
@@ -426,7 +427,10 @@ int plan_dilation_round(vo_ctx *ctx, vo_batch *b, std::vector<DilPlan> &dils, bo
   }
   int ka = fast_union_cap(segs / std::max(cols, 1.0)), fby = 4, persistent = 1;
   run_pending(ctx, b);  // tuning reads the dilation inputs
-  rc = tune_shape(ctx, b, dils, dvols, ka, &ka, &fby, &persistent);
+  // a round of one dilation passes its arguments as a kernel parameter
+  const bool one = hv.size() == 1;
+  const FastArgs a1 = hv[0].A;
+  rc = tune_shape(ctx, b, dils, dvols, one ? &a1 : nullptr, ka, &ka, &fby, &persistent);
   if (rc) return rc;
   const std::vector<int2> q = build_queue(dils, fby);
   int2 *dq = nullptr;
@@ -434,7 +438,7 @@ int plan_dilation_round(vo_ctx *ctx, vo_batch *b, std::vector<DilPlan> &dils, bo
   if (rc) return rc;
   cudaMemcpyAsync(dq, q.data(), sizeof(int2) * q.size(), cudaMemcpyHostToDevice, ctx->stream);
   VO_CK(ctx, cudaStreamSynchronize(ctx->stream));
-  const int per_sm = std::max(1, fast_batched_blocks_per_sm(ka, fby));
+  const int per_sm = std::max(1, fast_batched_blocks_per_sm(ka, fby, one));
   const int grid = persistent ? std::max(1, std::min<int>((int)q.size(), sms * per_sm)) : std::max(1, (int)q.size());
   std::vector<int *> counters;  // reset before every replay
   for (DilPlan &d : dils) {
@@ -445,7 +449,7 @@ int plan_dilation_round(vo_ctx *ctx, vo_batch *b, std::vector<DilPlan> &dils, bo
   record(b, 2, [=](cudaStream_t st) {
     cudaMemsetAsync(dnext, 0, sizeof(int), st);
     for (int *s : counters) cudaMemsetAsync(s, 0, sizeof(int), st);
-    fast_batched_launch(ka, fby, grid, st, dvols, dq, nq, dnext);
+    fast_batched_launch(ka, fby, grid, st, dvols, dq, nq, dnext, one ? &a1 : nullptr);
     fast_batched_mid_launch(st, dvols, nv, gmid);
   });
   b->stats.tile_rows = fby;
@@ -688,8 +692,14 @@ int vo_batch_run(vo_ctx *ctx, vo_batch *b, vo_timings *tm) {
   cudaEventElapsedTime(&graph_ms, ctx->ev[0], ctx->ev[1]);
   int reruns = 0;
   const int launches0 = ctx->launches;
+  b->stats.rerun_first = -1;
+  b->stats.rerun_cause = 0;
   for (int v = 0; v < n; ++v) {
     if (!flags[v] && !flags[n]) continue;
+    if (reruns == 0) {
+      b->stats.rerun_first = v;
+      b->stats.rerun_cause = (flags[v] ? 1 : 0) | (flags[n] ? 2 : 0);
+    }
     ++reruns;
     const int rc = rerun_volume(ctx, b, v, &b->rerun[v]);
     if (rc) return rc;

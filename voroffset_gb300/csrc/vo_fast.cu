@@ -612,10 +612,13 @@ __device__ __forceinline__ int place_union(const BatchVol &V, int x, int y, int 
 // by decreasing estimated work, so uneven volumes balance across the SMs.
 // Each column's union goes to its slot (place_union); a union of more than
 // KA intervals is listed for k_fast_batched_mid.
+// SINGLE: the round has one dilation, whose arguments come as the kernel
+// parameter A1 (constant bank) instead of from memory.
 // (At most 85 registers per thread: 768 / (kFB * FBY) blocks per SM.)
-template <int KA, int FBY>
+template <int KA, int FBY, bool SINGLE>
 __global__ void __launch_bounds__(kFB *FBY, 768 / (kFB * FBY)) k_fast_batched(const BatchVol *vols,
-                                                                               const int2 *queue, int nq, int *next) {
+                                                                               const int2 *queue, int nq, int *next,
+                                                                               const FastArgs A1) {
   extern __shared__ float2 sv_dyn[];
   __shared__ int s_item;
   __shared__ BatchVol s_vol;  // the item's arguments, read by every thread in the hot loop
@@ -642,7 +645,8 @@ __global__ void __launch_bounds__(kFB *FBY, 768 / (kFB * FBY)) k_fast_batched(co
       const int c = x + nx * y;
       UnionIds<KA> U;
       const unsigned mask = __activemask();
-      int n = fast_column<KA>(V.A, *V.A.E, x, y, sv_dyn + tid, kFB * FBY, U, mask);
+      const FastArgs &A = SINGLE ? A1 : V.A;
+      int n = fast_column<KA>(A, *A.E, x, y, sv_dyn + tid, kFB * FBY, U, mask);
       int dst = 0;
       if (n < 0) {
         V.mid_list[atomicAdd(V.mid_count, 1)] = c;
@@ -653,7 +657,7 @@ __global__ void __launch_bounds__(kFB *FBY, 768 / (kFB * FBY)) k_fast_batched(co
           dst = 0;
           n = 0;
         } else {
-          write_union(V.A, U, n, V.oz + dst);
+          write_union(A, U, n, V.oz + dst);
         }
       }
       V.obeg[c] = dst;
@@ -874,42 +878,59 @@ template <int KA>
 void *batched_kernel(int fby) {
   switch (fby) {
     case 1:
-      return reinterpret_cast<void *>(&k_fast_batched<KA, 1>);
+      return reinterpret_cast<void *>(&k_fast_batched<KA, 1, false>);
     case 2:
-      return reinterpret_cast<void *>(&k_fast_batched<KA, 2>);
+      return reinterpret_cast<void *>(&k_fast_batched<KA, 2, false>);
     case 4:
-      return reinterpret_cast<void *>(&k_fast_batched<KA, 4>);
+      return reinterpret_cast<void *>(&k_fast_batched<KA, 4, false>);
     case 8:
-      return reinterpret_cast<void *>(&k_fast_batched<KA, 8>);
+      return reinterpret_cast<void *>(&k_fast_batched<KA, 8, false>);
   }
   return nullptr;
 }
-void *batched_kernel(int ka, int fby) {
+template <int KA>
+void *batched_kernel_single(int fby) {
+  switch (fby) {
+    case 1:
+      return reinterpret_cast<void *>(&k_fast_batched<KA, 1, true>);
+    case 2:
+      return reinterpret_cast<void *>(&k_fast_batched<KA, 2, true>);
+    case 4:
+      return reinterpret_cast<void *>(&k_fast_batched<KA, 4, true>);
+    case 8:
+      return reinterpret_cast<void *>(&k_fast_batched<KA, 8, true>);
+  }
+  return nullptr;
+}
+void *batched_kernel(int ka, int fby, bool single) {
+  if (single)
+    return ka == 64 ? batched_kernel_single<64>(fby)
+                    : ka == 32 ? batched_kernel_single<32>(fby) : ka == 24 ? batched_kernel_single<24>(fby) : nullptr;
   return ka == 64 ? batched_kernel<64>(fby) : ka == 32 ? batched_kernel<32>(fby) : ka == 24 ? batched_kernel<24>(fby) : nullptr;
 }
 
-template <int KA>
+template <int KA, bool SINGLE>
 void launch_batched(int fby, int grid, size_t smem, cudaStream_t st, const BatchVol *vols, const int2 *queue, int nq,
-                    int *next) {
+                    int *next, const FastArgs &a1) {
   const dim3 blk(kFB, fby);
   switch (fby) {
     case 1:
-      k_fast_batched<KA, 1><<<grid, blk, smem, st>>>(vols, queue, nq, next);
+      k_fast_batched<KA, 1, SINGLE><<<grid, blk, smem, st>>>(vols, queue, nq, next, a1);
       break;
     case 2:
-      k_fast_batched<KA, 2><<<grid, blk, smem, st>>>(vols, queue, nq, next);
+      k_fast_batched<KA, 2, SINGLE><<<grid, blk, smem, st>>>(vols, queue, nq, next, a1);
       break;
     case 4:
-      k_fast_batched<KA, 4><<<grid, blk, smem, st>>>(vols, queue, nq, next);
+      k_fast_batched<KA, 4, SINGLE><<<grid, blk, smem, st>>>(vols, queue, nq, next, a1);
       break;
     default:
-      k_fast_batched<KA, 8><<<grid, blk, smem, st>>>(vols, queue, nq, next);
+      k_fast_batched<KA, 8, SINGLE><<<grid, blk, smem, st>>>(vols, queue, nq, next, a1);
   }
 }
 }  // namespace
 
-int fast_batched_blocks_per_sm(int ka, int fby) {
-  void *f = batched_kernel(ka, fby);
+int fast_batched_blocks_per_sm(int ka, int fby, bool single) {
+  void *f = batched_kernel(ka, fby, single);
   if (!f) return 0;
   const size_t smem = sizeof(float2) * ka * kFB * fby;
   if (smem > 227 * 1024 ||
@@ -926,15 +947,27 @@ int fast_batched_blocks_per_sm(int ka, int fby) {
 }
 
 int fast_batched_launch(int ka, int fby, int grid, cudaStream_t st, const BatchVol *vols, const int2 *queue, int nq,
-                        int *next) {
+                        int *next, const FastArgs *single) {
   if ((ka != 24 && ka != 32 && ka != 64) || (fby != 1 && fby != 2 && fby != 4 && fby != 8)) return VO_EINVAL;
   const size_t smem = sizeof(float2) * ka * kFB * fby;
-  if (ka == 64)
-    launch_batched<64>(fby, grid, smem, st, vols, queue, nq, next);
-  else if (ka == 32)
-    launch_batched<32>(fby, grid, smem, st, vols, queue, nq, next);
-  else
-    launch_batched<24>(fby, grid, smem, st, vols, queue, nq, next);
+  FastArgs none;
+  std::memset(&none, 0, sizeof none);
+  const FastArgs &a1 = single ? *single : none;
+  if (single) {
+    if (ka == 64)
+      launch_batched<64, true>(fby, grid, smem, st, vols, queue, nq, next, a1);
+    else if (ka == 32)
+      launch_batched<32, true>(fby, grid, smem, st, vols, queue, nq, next, a1);
+    else
+      launch_batched<24, true>(fby, grid, smem, st, vols, queue, nq, next, a1);
+  } else {
+    if (ka == 64)
+      launch_batched<64, false>(fby, grid, smem, st, vols, queue, nq, next, a1);
+    else if (ka == 32)
+      launch_batched<32, false>(fby, grid, smem, st, vols, queue, nq, next, a1);
+    else
+      launch_batched<24, false>(fby, grid, smem, st, vols, queue, nq, next, a1);
+  }
   return VO_OK;
 }
 

@@ -223,9 +223,11 @@ int fast_union_cap(double mean_segments_per_column);
 // Launch of the persistent kernel with union capacity ka (24, 32 or 64) and `fby`
 // rows of kFastCols columns per block (fby in {1, 2, 4, 8});
 // fast_batched_blocks_per_sm is the occupancy of that shape (0: unusable).
+// single: the round's one dilation's arguments (passed as a kernel
+// parameter), or nullptr for a round of several dilations.
 int fast_batched_launch(int ka, int fby, int grid, cudaStream_t st, const BatchVol *vols, const int2 *queue, int nq,
-                        int *next);
-int fast_batched_blocks_per_sm(int ka, int fby);
+                        int *next, const FastArgs *single);
+int fast_batched_blocks_per_sm(int ka, int fby, bool single);
 // Second tier of a batch round over the dilations vols[0..nv) (grid-stride).
 void fast_batched_mid_launch(cudaStream_t st, const BatchVol *vols, int nv, int grid);
 constexpr int kFastCols = 32;  // columns per block row
