@@ -142,7 +142,9 @@ typedef struct {
   int32_t learned;      /* 1 when slots and queue came from a sizer */
   int32_t reruns;       /* volumes re-run by the last vo_batch_run */
   int32_t rerun_first;  /* index of the first of them (-1: none) */
-  int32_t rerun_cause;  /* its overflow flags: 1 union beyond the second tier or spill exhausted, 2 complement slot */
+  int32_t rerun_cause;  /* its overflow flags: 1 union beyond the FP64 list, 2 complement slot, 4 spill exhausted */
+  double spill_peak;    /* largest fraction of a dilation's spill region used by the last run (> 1: exhausted) */
+  int32_t spill_peak_round; /* its dilation round */
   double plan_ms;       /* host time of vo_batch_create */
   double tune_ms[4];    /* autotuner sample times for 1, 2, 4, 8 rows at the largest union capacity tried (0: cached) */
 } vo_batch_stats;

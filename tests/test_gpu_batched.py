@@ -50,8 +50,9 @@ def test_batched_equals_single_calls(ctx, vo):
 
 
 def test_batched_overflow_reruns(ctx, vo, oracle):
-    # 150 thin plates per column: more union intervals than the second tier holds
-    nx, ny, k = 24, 20, 150
+    # 40 thin plates in every column: each union outgrows the fixed 32-interval
+    # slot, the spill region runs out, and the volume re-runs on its own
+    nx, ny, k = 24, 20, 40
     base = np.arange(k, dtype=np.float64) * 3.0
     z = np.tile(np.stack([base, base + 1.0], 1).reshape(-1), nx * ny)
     offs = (np.arange(nx * ny + 1) * k).astype(np.int32)
@@ -129,3 +130,24 @@ def test_plan_with_more_radii_than_the_table_cache(ctx, vo, oracle):
         b.run()
         for (g, o, z, r, op), out in zip(items, b.outputs()):
             assert_same(ctx.download(out), oracle.morph(ogrid(oracle, g), o, z, r, op), tol=0.0, what=f"{op} r={r}")
+
+
+def test_batched_third_tier_without_rerun(ctx, vo, oracle):
+    """A few columns with 150-interval unions: the FP64 third tier computes them
+    inside the replay and the spill region takes them, so no volume re-runs."""
+    nx, ny, k = 64, 48, 150
+    g0, o0, z0 = vo.synth_volume(vo.SynthSpec(64, n_spheres=30, s_rmin=2, s_rmax=8, seed=8, ny=48, zmax=200))
+    cols = [z0[2 * o0[c]:2 * o0[c + 1]] for c in range(nx * ny)]
+    base = 300.0 + np.arange(k) * 3.0
+    plates = np.stack([base, base + 1.0], 1).reshape(-1)
+    for x in range(30, 36):
+        cols[x + nx * 20] = np.concatenate([cols[x + nx * 20], plates])
+    offs = np.zeros(nx * ny + 1, np.int32)
+    offs[1:] = np.cumsum([c.size // 2 for c in cols])
+    z = np.concatenate(cols)
+    g = vo.Grid(nx, ny, (0, 0, 0), (nx, ny, 800), 1.0, 0)
+    v = ctx.upload(g, offs, z)
+    for op in ("dilation", "closing"):
+        outs, t = ctx.morph_batched([v], [op], [0.9], "fast")
+        assert t["overflow_columns"] == 0, op
+        assert_same(ctx.download(outs[0]), oracle.morph(ogrid(oracle, g), offs, z, 0.9, op), tol=0.0, what=op)

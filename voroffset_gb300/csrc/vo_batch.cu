@@ -24,7 +24,8 @@
 // Then the closures are captured into one graph. vo_batch_run replays it and
 // re-runs, through the single-volume path, every volume whose overflow flag
 // is set (a union larger than its slot with the spill region exhausted, or
-// larger than kUnionCapMid), so results never depend on the predictions.
+// beyond the FP64 third tier's list), so results never depend on the
+// predictions.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -68,6 +69,7 @@ struct DilPlan {
   unsigned int *maxbits = nullptr;
   int2 *pairs = nullptr;
   int *mid_list = nullptr, *mid_count = nullptr;
+  int *big_list = nullptr, *big_count = nullptr;
   int npairs = 0;
   int32_t *tcap = nullptr, *toff = nullptr;
   int tiles32_x = 0, tiles32 = 0;
@@ -94,7 +96,14 @@ struct vo_batch {
   std::vector<void *> dmem;            // device allocations of the plan
   std::vector<SlotVol> owned;
   std::vector<SlotVol> finals;
-  int *d_flags = nullptr;  // [v]: overflow of volume v, [n]: complement slot overflow
+  int *d_flags = nullptr;  // [v]: overflow flags of volume v, [n]: complement slot overflow
+  double2 *big_scratch = nullptr;  // working lists of the FP64 third tier
+  struct Spill {
+    int *used;
+    int cap, round;
+  };
+  std::vector<Spill> spills;  // per dilation: spill counter and capacity
+  int rounds = 0;             // dilation rounds
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   std::vector<vo_volume *> rerun;
@@ -226,6 +235,8 @@ BatchVol batch_vol(const DilPlan &d, int *ovf) {
   v.spill_used = d.spill_used;
   v.mid_list = d.mid_list;
   v.mid_count = d.mid_count;
+  v.big_list = d.big_list;
+  v.big_count = d.big_count;
   v.ovf = ovf;
   return v;
 }
@@ -337,6 +348,7 @@ int tune_shape(vo_ctx *ctx, vo_batch *b, const std::vector<DilPlan> &dils, const
       for (const DilPlan &d : dils) {
         cudaMemsetAsync(d.spill_used, 0, sizeof(int), ctx->stream);
         cudaMemsetAsync(d.mid_count, 0, sizeof(int), ctx->stream);
+        cudaMemsetAsync(d.big_count, 0, sizeof(int), ctx->stream);
       }
       cudaEventRecord(ctx->ev[2], ctx->stream);
       fast_batched_launch(ka, fby, grid, ctx->stream, dvols, dq, (int)sample.size(), dnext, single);
@@ -384,6 +396,8 @@ int plan_dilation_round(vo_ctx *ctx, vo_batch *b, std::vector<DilPlan> &dils, bo
     if (!rc) rc = plan_alloc(ctx, b, &d.prec, pairs.size());
     if (!rc) rc = plan_alloc(ctx, b, &d.mid_list, (size_t)ncols);
     if (!rc) rc = plan_alloc(ctx, b, &d.mid_count, 1);
+    if (!rc) rc = plan_alloc(ctx, b, &d.big_list, (size_t)ncols);
+    if (!rc) rc = plan_alloc(ctx, b, &d.big_count, 1);
     if (!rc) rc = plan_alloc(ctx, b, &d.maxbits, 1);
     if (!rc) rc = plan_alloc(ctx, b, &d.pairs, pairs.size());
     if (rc) return rc;
@@ -444,14 +458,23 @@ int plan_dilation_round(vo_ctx *ctx, vo_batch *b, std::vector<DilPlan> &dils, bo
   for (DilPlan &d : dils) {
     counters.push_back(d.spill_used);
     counters.push_back(d.mid_count);
+    counters.push_back(d.big_count);
   }
+  if (!b->big_scratch) {
+    rc = plan_alloc(ctx, b, &b->big_scratch, fast_batched_big_scratch_elems(sms));
+    if (rc) return rc;
+  }
+  double2 *big_scratch = b->big_scratch;
   const int nq = (int)q.size(), nv = (int)dils.size(), gmid = sms * 16;
-  record(b, 2, [=](cudaStream_t st) {
+  record(b, 3, [=](cudaStream_t st) {
     cudaMemsetAsync(dnext, 0, sizeof(int), st);
     for (int *s : counters) cudaMemsetAsync(s, 0, sizeof(int), st);
     fast_batched_launch(ka, fby, grid, st, dvols, dq, nq, dnext, one ? &a1 : nullptr);
     fast_batched_mid_launch(st, dvols, nv, gmid);
+    fast_batched_big_launch(st, dvols, nv, sms, big_scratch);
   });
+  for (const DilPlan &d : dils) b->spills.push_back({d.spill_used, d.spill_cap, b->rounds});
+  ++b->rounds;
   b->stats.tile_rows = fby;
   b->stats.union_cap = ka;
   b->stats.persistent = persistent;
@@ -690,6 +713,18 @@ int vo_batch_run(vo_ctx *ctx, vo_batch *b, vo_timings *tm) {
   VO_CK(ctx, cudaStreamSynchronize(ctx->stream));
   float graph_ms = 0;
   cudaEventElapsedTime(&graph_ms, ctx->ev[0], ctx->ev[1]);
+  // spill use of every dilation (the largest fraction and its round)
+  b->stats.spill_peak = 0;
+  b->stats.spill_peak_round = -1;
+  for (const auto &sp : b->spills) {
+    int used = 0;
+    if (cudaMemcpy(&used, sp.used, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) break;
+    const double f = sp.cap > 0 ? (double)used / sp.cap : 0.0;
+    if (f > b->stats.spill_peak) {
+      b->stats.spill_peak = f;
+      b->stats.spill_peak_round = sp.round;
+    }
+  }
   int reruns = 0;
   const int launches0 = ctx->launches;
   b->stats.rerun_first = -1;
@@ -698,7 +733,7 @@ int vo_batch_run(vo_ctx *ctx, vo_batch *b, vo_timings *tm) {
     if (!flags[v] && !flags[n]) continue;
     if (reruns == 0) {
       b->stats.rerun_first = v;
-      b->stats.rerun_cause = (flags[v] ? 1 : 0) | (flags[n] ? 2 : 0);
+      b->stats.rerun_cause = flags[v] | (flags[n] ? 2 : 0);
     }
     ++reruns;
     const int rc = rerun_volume(ctx, b, v, &b->rerun[v]);

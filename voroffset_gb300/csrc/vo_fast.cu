@@ -601,7 +601,7 @@ __device__ __forceinline__ int place_union(const BatchVol &V, int x, int y, int 
   if (n > cap) {
     const int off = atomicAdd(V.spill_used, n);
     if (off + n <= V.spill_cap) return V.spill_base + off;
-    atomicOr(V.ovf, 1);
+    atomicOr(V.ovf, 4);  // spill region exhausted
     return -1;
   }
   return dst;
@@ -682,7 +682,57 @@ __global__ void __launch_bounds__(kMidThreads) k_fast_batched_mid(const BatchVol
       const unsigned mask = __activemask();
       int n = fast_column<kKM>(V.A, *V.A.E, x, y, sv + threadIdx.x, kMidThreads, U, mask);
       int dst = -1;
-      if (n < 0)
+      if (n < 0) {
+        V.big_list[atomicAdd(V.big_count, 1)] = c;  // third tier
+        n = 0;
+        dst = 0;
+      } else {
+        dst = place_union(V, x, y, n);
+      }
+      if (dst < 0) {
+        dst = 0;
+        n = 0;
+      } else if (n > 0) {
+        write_union(V.A, U, n, V.oz + dst);
+      }
+      V.obeg[c] = dst;
+      V.oend[c] = dst + n;
+    }
+  }
+}
+
+// Third tier of a batch round (FP64, grid-stride): the columns whose union
+// exceeds kKM, each built in a kBigCap-interval list in global scratch and
+// placed like the other tiers; a union beyond kBigCap sets the overflow flag.
+__global__ void __launch_bounds__(kBigThreads) k_fast_batched_big(const BatchVol *vols, int nv, double2 *scratch) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+  double2 *L = scratch + (size_t)tid * kBigCap;
+  for (int v = 0; v < nv; ++v) {
+    const BatchVol &V = vols[v];
+    const FastArgs &A = V.A;
+    const int m = *V.big_count;
+    for (int i = tid; i < m; i += nth) {
+      const int c = V.big_list[i];
+      const int x = c % A.nx, y = c / A.nx;
+      int n = 0;
+      bool ok = true;
+      for (int p = 0; p < A.npairs && ok; ++p) {
+        const int2 ad = A.pairs[p];
+        const int a = ad.x, d = ad.y;
+        const double h = A.H64[d * A.W + a];
+        for (int s = 0; s < 4 && ok; ++s) {
+          const int xs = (s & 1) ? x + a : x - a;
+          const int ys = (s & 2) ? y + d : y - d;
+          if ((s & 1) && a == 0) continue;
+          if ((s & 2) && d == 0) continue;
+          if (xs < 0 || xs >= A.nx || ys < 0 || ys >= A.ny) continue;
+          const int cs = xs + A.nx * ys;
+          for (int k = A.beg[cs]; k < A.end[cs] && ok; ++k)
+            ok = big_insert(L, n, kBigCap, __dsub_rn(A.zd[2 * k], h), __dadd_rn(A.zd[2 * k + 1], h));
+        }
+      }
+      int dst = -1;
+      if (!ok)
         atomicOr(V.ovf, 1);
       else
         dst = place_union(V, x, y, n);
@@ -690,7 +740,7 @@ __global__ void __launch_bounds__(kMidThreads) k_fast_batched_mid(const BatchVol
         dst = 0;
         n = 0;
       } else {
-        write_union(V.A, U, n, V.oz + dst);
+        for (int k = 0; k < n; ++k) V.oz[dst + k] = L[k];
       }
       V.obeg[c] = dst;
       V.oend[c] = dst + n;
@@ -973,6 +1023,12 @@ int fast_batched_launch(int ka, int fby, int grid, cudaStream_t st, const BatchV
 
 void fast_batched_mid_launch(cudaStream_t st, const BatchVol *vols, int nv, int grid) {
   k_fast_batched_mid<<<grid, kMidThreads, 0, st>>>(vols, nv);
+}
+
+size_t fast_batched_big_scratch_elems(int grid) { return (size_t)grid * kBigThreads * kBigCap; }
+
+void fast_batched_big_launch(cudaStream_t st, const BatchVol *vols, int nv, int grid, double2 *scratch) {
+  k_fast_batched_big<<<grid, kBigThreads, 0, st>>>(vols, nv, scratch);
 }
 
 }  // namespace vo

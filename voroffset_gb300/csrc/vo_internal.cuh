@@ -201,8 +201,9 @@ struct BatchVol {
   int tiles32_x;
   int spill_base, spill_cap;
   int *spill_used;
-  int *mid_list, *mid_count;  // columns whose union exceeds kUnionCap (second tier)
-  int *ovf;  // set when a column's union does not fit (slot + spill, or kUnionCapMid)
+  int *mid_list, *mid_count;  // columns whose union exceeds the main capacity (second tier)
+  int *big_list, *big_count;  // columns whose union exceeds kUnionCapMid (third tier, FP64)
+  int *ovf;  // flags: 1 a union beyond the FP64 list, 4 spill region exhausted
 };
 
 // Fills DeviceTables::dH from H on the device (directed rounding).
@@ -230,6 +231,10 @@ int fast_batched_launch(int ka, int fby, int grid, cudaStream_t st, const BatchV
 int fast_batched_blocks_per_sm(int ka, int fby, bool single);
 // Second tier of a batch round over the dilations vols[0..nv) (grid-stride).
 void fast_batched_mid_launch(cudaStream_t st, const BatchVol *vols, int nv, int grid);
+// Third tier (FP64) of a batch round; scratch holds
+// fast_batched_big_scratch_elems(grid) intervals.
+size_t fast_batched_big_scratch_elems(int grid);
+void fast_batched_big_launch(cudaStream_t st, const BatchVol *vols, int nv, int grid, double2 *scratch);
 constexpr int kFastCols = 32;  // columns per block row
 
 // Batch plans (vo_batch.cu).

@@ -6,7 +6,8 @@ Every training volume is a seeded synthetic union of spheres (uniform or
 lognormal radii) and cylinders on a 64..256 square grid with a z-range up to
 4096 dexels (object densities per dexel^3 over two decades); half of them are
 replaced by their complement with a one-column border (the input the erosion
-chain dilates). Each is dilated by the FP32-guarded GPU method at a radius in
+chain dilates), and every third one also contributes the complement of its
+dilation (the input of a closing's second dilation). Each is dilated by the FP32-guarded GPU method at a radius in
 [2, 64] (multiples of 0.25), and the per-tile features of the input and the
 targets from the result (vo_sizer_tile_features / vo_sizer_tile_targets)
 form one sample per 32 x 32 tile. Training is full-batch Adam on the device
@@ -30,7 +31,9 @@ WEIGHTS = os.path.join(HERE, "sizer_weights.f32")
 
 def complement(grid: Grid, offs: np.ndarray, z: np.ndarray):
     """Complement of every column on [zmin, zmax] with a border of full columns
-    (the shape of the erosion chain's dilation input, Voronoi.cpp:38-70)."""
+    (the shape of the erosion chain's dilation input, Voronoi.cpp:38-70,
+    negate_ray of MorphologyOperators.cpp:230-259, without its rare drop of a
+    value equal to zmin or zmax)."""
     zmin = grid.origin[2] / grid.spacing - 1
     zmax = grid.origin[2] / grid.spacing + 2 * grid.padding + grid.extent[2] / grid.spacing + 1
     nx, ny = grid.nx, grid.ny
@@ -42,12 +45,38 @@ def complement(grid: Grid, offs: np.ndarray, z: np.ndarray):
     vals[1::2] = zmax
     zc = np.insert(z, idx, vals)
     cnt = np.diff(offs) + 1
-    # keep non-empty intervals only
     pairs = zc.reshape(-1, 2)
-    keep = pairs[:, 1] > pairs[:, 0]
     col = np.repeat(np.arange(nx * ny), cnt)
-    pairs = pairs[keep]
-    cnt = np.bincount(col[keep], minlength=nx * ny).reshape(ny, nx)
+    # An inverted pair [a, b], a > b, is left where a column's values exceed
+    # [zmin, zmax]; like the method (and the reference's pass 2, which sees its
+    # two endpoints), rewrite it as the points [b, b] and [a, a], then sort and
+    # merge that column as closed intervals. Empty pairs of other columns are
+    # kept as they are.
+    inv = pairs[:, 0] > pairs[:, 1]
+    if inv.any():
+        bad = np.unique(col[inv])
+        starts = np.concatenate([[0], np.cumsum(cnt)])
+        fixed_pairs, fixed_cols = [], []
+        for c in bad:
+            seg = pairs[starts[c]:starts[c + 1]]
+            pts = []
+            for a, b in seg:
+                pts += [(b, b), (a, a)] if a > b else [(a, b)]
+            pts.sort()
+            merged = []
+            for a, b in pts:
+                if merged and not (merged[-1][1] < a):
+                    merged[-1][1] = max(merged[-1][1], b)
+                else:
+                    merged.append([a, b])
+            fixed_pairs += merged
+            fixed_cols += [c] * len(merged)
+        drop = np.isin(col, bad)
+        pairs = np.concatenate([pairs[~drop], np.array(fixed_pairs).reshape(-1, 2)])
+        col = np.concatenate([col[~drop], np.array(fixed_cols, dtype=col.dtype)])
+        order = np.argsort(col, kind="stable")
+        pairs, col = pairs[order], col[order]
+    cnt = np.bincount(col, minlength=nx * ny).reshape(ny, nx)
     # bordered grid (nx+2) x (ny+2): interior (x+1, y+1) <- (x, y); border columns full
     full = np.zeros((ny + 2, nx + 2), np.int64) + 1
     full[1:-1, 1:-1] = cnt
@@ -87,6 +116,9 @@ def make_volume(rng: np.random.Generator):
 
 
 def generate(ctx: Context, n: int, seed: int, log_every: int = 0):
+    """Features and targets of n generated volumes. Every third one also adds
+    the second dilation of a closing: the complement (with border) of the
+    first dilation's result, dilated by the same radius."""
     rng = np.random.default_rng(seed)
     sz = ctx.sizer(seed=1)
     feats, targs = [], []
@@ -96,6 +128,15 @@ def generate(ctx: Context, n: int, seed: int, log_every: int = 0):
         out, _ = ctx.morph(v, "dilation", r, "fast")
         feats.append(sz.features(v, r))
         targs.append(sz.targets(v, out, r))
+        if i % 3 == 2:
+            o1, z1 = ctx.download(out)
+            g2, o2, z2 = complement(g, o1, z1)
+            v2 = ctx.upload(g2, o2, z2)
+            out2, _ = ctx.morph(v2, "dilation", r, "fast")
+            feats.append(sz.features(v2, r))
+            targs.append(sz.targets(v2, out2, r))
+            out2.free()
+            v2.free()
         out.free()
         v.free()
         if log_every and (i + 1) % log_every == 0:
