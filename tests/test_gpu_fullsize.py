@@ -73,3 +73,37 @@ def test_fullsize_plain_matches_fast(ctx, vo, spheres_cyl2048):
     ao, az = ctx.download(a)
     bo, bz = ctx.download(b)
     assert np.array_equal(ao, bo) and np.array_equal(az, bz)
+
+
+@pytest.mark.parametrize("op", ["dilation", "erosion", "opening", "closing"])
+def test_config_spheres1024_all_ops_fast_equals_plain(ctx, vo, op):
+    """1024^2 grid, 4096 spheres (radii 4-40), r = 32: the FP32-guarded method,
+    single-volume and as a batch plan, equals the FP64 plain method bit for bit
+    for every operation (the plain method equals the oracle on the parity
+    suites)."""
+    grid, offs, z = vo.workload("spheres1024", seed=1)
+    v = ctx.upload(grid, offs, z)
+    a, _ = ctx.morph(v, op, 32.0, "separable")
+    b, _ = ctx.morph(v, op, 32.0, "fast")
+    outs, t = ctx.morph_batched([v], [op], [32.0], "fast")
+    ao, az = ctx.download(a)
+    for other in (b, outs[0]):
+        oo, oz = ctx.download(other)
+        assert np.array_equal(ao, oo) and np.array_equal(az, oz), op
+
+
+def test_config_torus_dexelize_and_dilate(ctx, vo, oracle):
+    """The torus configuration: 256 x 64 quads (32768 triangles) displaced by
+    seeded noise, -n 256 -p 10, dilation r = 8: the GPU rasteriser equals the
+    oracle's, and so do the dilations (FP64 and FP32 methods), bit for bit."""
+    verts, tris = vo.synth_torus(256, 64, 0.30, 0.10, 0.01, seed=1)
+    og, offs, z = oracle.dexelize(verts, tris, num_dexels=256, padding=10)
+    v = ctx.dexelize(verts, tris, num_dexels=256, padding=10)
+    got = ctx.download(v)
+    assert np.array_equal(got[0], offs) and np.array_equal(got[1], z)
+    want = oracle.morph(og, offs, z, 8.0, "dilation")
+    for method in ("separable", "fast"):
+        out, _ = ctx.morph(v, "dilation", 8.0, method)
+        o, zz = ctx.download(out)
+        assert np.array_equal(o, want[0]) and np.array_equal(zz, want[1]), method
+    assert ctx.xor_volume(out, out) == 0.0
