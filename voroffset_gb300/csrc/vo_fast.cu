@@ -614,9 +614,10 @@ __device__ __forceinline__ int place_union(const BatchVol &V, int x, int y, int 
 // KA intervals is listed for k_fast_batched_mid.
 // SINGLE: the round has one dilation, whose arguments come as the kernel
 // parameter A1 (constant bank) instead of from memory.
-// (At most 73 registers per thread: 896 / (kFB * FBY) blocks per SM.)
+// (At most 64 registers per thread: 1024 / (kFB * FBY) blocks per SM; the
+// occupancy outweighs the spills, measured on the 2048^2 r=32 dilation.)
 template <int KA, int FBY, bool SINGLE>
-__global__ void __launch_bounds__(kFB *FBY, 896 / (kFB * FBY)) k_fast_batched(const BatchVol *vols,
+__global__ void __launch_bounds__(kFB *FBY, 1024 / (kFB * FBY)) k_fast_batched(const BatchVol *vols,
                                                                                const int2 *queue, int nq, int *next,
                                                                                const FastArgs A1) {
   extern __shared__ float2 sv_dyn[];
