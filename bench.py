@@ -310,7 +310,7 @@ def batch_main(args, rank, world, local):
                        "rerun": rerun,
                        "columns": cols, "method": "batched+learned" if sizer else "batched",
                        "ops": {o: ops.count(o) for o in set(ops)},
-                       "plan": {k: st[k] for k in ("slot_bytes", "tiles", "tile_rows", "union_cap", "persistent", "graph_nodes",
+                       "plan": {k: st[k] for k in ("slot_bytes", "tiles", "tile_rows", "union_cap", "persistent", "regs", "graph_nodes",
                                                    "graph_kernels", "learned", "plan_ms", "tune_ms")},
                        "reruns_per_step": acc["reruns"] / (args.steps + args.warmup)},
             "gpu_launches": int(acc["launches"] * args.steps / (args.steps + args.warmup)),
@@ -491,7 +491,7 @@ def main():
            "in_segments": int(offs[-1]), "out_segments": int(out_segs), "mid_pieces": int(mid),
            "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas" if world > 1 else "single GPU"}
     if plan_stats is not None:
-        cfg["plan"] = {k: plan_stats[k] for k in ("slot_bytes", "tiles", "tile_rows", "union_cap", "persistent", "graph_nodes",
+        cfg["plan"] = {k: plan_stats[k] for k in ("slot_bytes", "tiles", "tile_rows", "union_cap", "persistent", "regs", "graph_nodes",
                                                   "graph_kernels", "learned", "plan_ms", "tune_ms")}
     line = {"metric": METRIC, "value": value, "unit": "Mcolumns/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,

@@ -134,9 +134,10 @@ typedef struct vo_batch vo_batch;
 typedef struct {
   int64_t slot_bytes;   /* output slot memory of the dilations */
   int32_t tiles;        /* work-queue items over all rounds */
-  int32_t tile_rows;    /* rows of 32 columns per block chosen by the autotuner (last round) */
+  int32_t tile_rows;    /* rows of 32 columns per block chosen by the autotuner (last round): 1, 2 or 4 */
   int32_t union_cap;    /* union intervals per column of the main kernel (last round): 24, 32 or 64 */
   int32_t persistent;   /* 1: one wave of blocks pulling queue items; 0: one block per item (last round) */
+  int32_t regs;         /* register budget per thread of the batch kernel (last round): 64 or 80 */
   int32_t graph_nodes;  /* nodes of the captured graph */
   int32_t graph_kernels;/* kernel launches per replay */
   int32_t learned;      /* 1 when slots and queue came from a sizer */
@@ -146,7 +147,8 @@ typedef struct {
   double spill_peak;    /* largest fraction of a dilation's spill region used by the last run (> 1: exhausted) */
   int32_t spill_peak_round; /* its dilation round */
   double plan_ms;       /* host time of vo_batch_create */
-  double tune_ms[4];    /* autotuner sample times for 1, 2, 4, 8 rows at the largest union capacity tried (0: cached) */
+  double tune_ms[4];    /* autotuner sample times for 1, 2, 4 rows (persistent, 64 registers, the largest union
+                           capacity tried; 0: cached); [3] unused */
 } vo_batch_stats;
 int vo_batch_create(vo_ctx *ctx, int n, const int *ops, const double *radii, int method,
                     const vo_volume *const *ins, vo_batch **out);

@@ -53,7 +53,7 @@ class _SynthParams(C.Structure):
 
 class _BatchStats(C.Structure):
     _fields_ = [("slot_bytes", C.c_int64), ("tiles", C.c_int32), ("tile_rows", C.c_int32),
-                ("union_cap", C.c_int32), ("persistent", C.c_int32), ("graph_nodes", C.c_int32), ("graph_kernels", C.c_int32), ("learned", C.c_int32),
+                ("union_cap", C.c_int32), ("persistent", C.c_int32), ("regs", C.c_int32), ("graph_nodes", C.c_int32), ("graph_kernels", C.c_int32), ("learned", C.c_int32),
                 ("reruns", C.c_int32), ("rerun_first", C.c_int32), ("rerun_cause", C.c_int32), ("spill_peak", C.c_double),
                 ("spill_peak_round", C.c_int32), ("plan_ms", C.c_double), ("tune_ms", C.c_double * 4)]
 

@@ -80,7 +80,8 @@ struct DilPlan {
   int64_t slot_entries = 0;
 };
 
-constexpr int kTuneShapes[] = {1, 2, 4, 8};
+constexpr int kTuneShapes[] = {1, 2, 4};
+constexpr int kTuneRegs[] = {64, 80};
 
 }  // namespace
 
@@ -281,8 +282,8 @@ int sm_count() {
   return sms > 0 ? sms : 1;
 }
 
-// Autotuner: times every (union capacity, block shape, persistent or one
-// block per item) on a sample of the round's queue (four evenly spaced
+// Autotuner: times every (union capacity, register budget, block shape,
+// persistent or one block per item) on a sample of the round's queue (four evenly spaced
 // contiguous runs, about 1/16 of it and at least 512 items), the second tier
 // included, and keeps the fastest per column. Results are cached in the
 // context per (one dilation or several, log2 columns, radius bucket, dense or
@@ -290,7 +291,8 @@ int sm_count() {
 // Tuning launches write into the round's output slots, which the real launch
 // overwrites.
 int tune_shape(vo_ctx *ctx, vo_batch *b, const std::vector<DilPlan> &dils, const BatchVol *dvols,
-               const FastArgs *single, int ka_hint, int *ka_out, int *fby_out, int *persistent_out) {
+               const FastArgs *single, int ka_hint, int *ka_out, int *fby_out, int *persistent_out,
+               int *regs_out) {
   int64_t cols = 0;
   double rmax = 0;
   for (const DilPlan &d : dils) {
@@ -304,11 +306,12 @@ int tune_shape(vo_ctx *ctx, vo_batch *b, const std::vector<DilPlan> &dils, const
       *ka_out = (kv.second >> 8) & 255;
       *fby_out = kv.second & 255;
       *persistent_out = (kv.second >> 16) & 1;
+      *regs_out = (kv.second >> 17) & 1 ? 80 : 64;
       return VO_OK;
     }
   // union capacities to try: 64 for dense inputs, else 24 and 32
   std::vector<int> kas = ka_hint == 64 ? std::vector<int>{64} : std::vector<int>{24, 32};
-  int best_ka = kas.back(), best_pers = 1;
+  int best_ka = kas.back(), best_pers = 1, best_regs = 64;
   const int sms = sm_count();
   int best = 4;
   double best_t = 1e300;
@@ -318,10 +321,11 @@ int tune_shape(vo_ctx *ctx, vo_batch *b, const std::vector<DilPlan> &dils, const
   size_t qcap = 0;
   const int gmid = sms * 16;
   for (int ka : kas)
+  for (int regs : kTuneRegs)
   for (int fby : kTuneShapes)
   for (int pers = 1; pers >= 0; --pers) {
     if (rc) break;
-    const int per_sm = fast_batched_blocks_per_sm(ka, fby, single != nullptr);
+    const int per_sm = fast_batched_blocks_per_sm(ka, fby, single != nullptr, regs);
     if (per_sm <= 0) continue;
     // four contiguous runs of the queue, evenly spaced: neighbouring tiles run
     // together as in the real launch, so the sample sees its cache reuse
@@ -351,7 +355,7 @@ int tune_shape(vo_ctx *ctx, vo_batch *b, const std::vector<DilPlan> &dils, const
         cudaMemsetAsync(d.big_count, 0, sizeof(int), ctx->stream);
       }
       cudaEventRecord(ctx->ev[2], ctx->stream);
-      fast_batched_launch(ka, fby, grid, ctx->stream, dvols, dq, (int)sample.size(), dnext, single);
+      fast_batched_launch(ka, fby, regs, grid, ctx->stream, dvols, dq, (int)sample.size(), dnext, single);
       fast_batched_mid_launch(ctx->stream, dvols, (int)dils.size(), gmid);  // unions beyond ka count too
       cudaEventRecord(ctx->ev[3], ctx->stream);
       cudaError_t e = cudaStreamSynchronize(ctx->stream);
@@ -363,21 +367,23 @@ int tune_shape(vo_ctx *ctx, vo_batch *b, const std::vector<DilPlan> &dils, const
     }
     if (rc) break;
     const double per_col = ms / ((double)sample.size() * kFastCols * fby);
-    if (ka == kas.back() && pers) b->stats.tune_ms[fby == 1 ? 0 : fby == 2 ? 1 : fby == 4 ? 2 : 3] = ms;
+    if (ka == kas.back() && pers && regs == 64) b->stats.tune_ms[fby == 1 ? 0 : fby == 2 ? 1 : 2] = ms;
     if (per_col < best_t) {
       best_t = per_col;
       best = fby;
       best_ka = ka;
       best_pers = pers;
+      best_regs = regs;
     }
   }
   dfree(ctx, dnext);
   dfree(ctx, dq);
   if (rc) return rc;
-  ctx->tune_cache.push_back({key, (best_pers << 16) | (best_ka << 8) | best});
+  ctx->tune_cache.push_back({key, ((best_regs == 80) << 17) | (best_pers << 16) | (best_ka << 8) | best});
   *ka_out = best_ka;
   *fby_out = best;
   *persistent_out = best_pers;
+  *regs_out = best_regs;
   return VO_OK;
 }
 
@@ -439,12 +445,12 @@ int plan_dilation_round(vo_ctx *ctx, vo_batch *b, std::vector<DilPlan> &dils, bo
     segs += d.in.owns ? 0.5 * d.in.cap * nc : (double)d.in.entries;
     cols += nc;
   }
-  int ka = fast_union_cap(segs / std::max(cols, 1.0)), fby = 4, persistent = 1;
+  int ka = fast_union_cap(segs / std::max(cols, 1.0)), fby = 4, persistent = 1, regs = 64;
   run_pending(ctx, b);  // tuning reads the dilation inputs
   // a round of one dilation passes its arguments as a kernel parameter
   const bool one = hv.size() == 1;
   const FastArgs a1 = hv[0].A;
-  rc = tune_shape(ctx, b, dils, dvols, one ? &a1 : nullptr, ka, &ka, &fby, &persistent);
+  rc = tune_shape(ctx, b, dils, dvols, one ? &a1 : nullptr, ka, &ka, &fby, &persistent, &regs);
   if (rc) return rc;
   const std::vector<int2> q = build_queue(dils, fby);
   int2 *dq = nullptr;
@@ -452,7 +458,7 @@ int plan_dilation_round(vo_ctx *ctx, vo_batch *b, std::vector<DilPlan> &dils, bo
   if (rc) return rc;
   cudaMemcpyAsync(dq, q.data(), sizeof(int2) * q.size(), cudaMemcpyHostToDevice, ctx->stream);
   VO_CK(ctx, cudaStreamSynchronize(ctx->stream));
-  const int per_sm = std::max(1, fast_batched_blocks_per_sm(ka, fby, one));
+  const int per_sm = std::max(1, fast_batched_blocks_per_sm(ka, fby, one, regs));
   const int grid = persistent ? std::max(1, std::min<int>((int)q.size(), sms * per_sm)) : std::max(1, (int)q.size());
   std::vector<int *> counters;  // reset before every replay
   for (DilPlan &d : dils) {
@@ -469,7 +475,7 @@ int plan_dilation_round(vo_ctx *ctx, vo_batch *b, std::vector<DilPlan> &dils, bo
   record(b, 3, [=](cudaStream_t st) {
     cudaMemsetAsync(dnext, 0, sizeof(int), st);
     for (int *s : counters) cudaMemsetAsync(s, 0, sizeof(int), st);
-    fast_batched_launch(ka, fby, grid, st, dvols, dq, nq, dnext, one ? &a1 : nullptr);
+    fast_batched_launch(ka, fby, regs, grid, st, dvols, dq, nq, dnext, one ? &a1 : nullptr);
     fast_batched_mid_launch(st, dvols, nv, gmid);
     fast_batched_big_launch(st, dvols, nv, sms, big_scratch);
   });
@@ -478,6 +484,7 @@ int plan_dilation_round(vo_ctx *ctx, vo_batch *b, std::vector<DilPlan> &dils, bo
   b->stats.tile_rows = fby;
   b->stats.union_cap = ka;
   b->stats.persistent = persistent;
+  b->stats.regs = regs;
   b->stats.tiles += nq;
   if (later_rounds) run_pending(ctx, b);
   return VO_OK;

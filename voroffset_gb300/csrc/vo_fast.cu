@@ -618,10 +618,11 @@ __device__ __forceinline__ int place_union(const BatchVol &V, int x, int y, int 
 // KA intervals is listed for k_fast_batched_mid.
 // SINGLE: the round has one dilation, whose arguments come as the kernel
 // parameter A1 (constant bank) instead of from memory.
-// (At most 64 registers per thread: 1024 / (kFB * FBY) blocks per SM; the
-// occupancy outweighs the spills, measured on the 2048^2 r=32 dilation.)
-template <int KA, int FBY, bool SINGLE>
-__global__ void __launch_bounds__(kFB *FBY, 1024 / (kFB * FBY)) k_fast_batched(const BatchVol *vols,
+// LBN / (kFB * FBY) blocks per SM bound the registers: LBN = 1024 gives 64
+// per thread (32 warps per SM, some spills), 768 gives 85 (24 warps); the
+// autotuner picks per round (the first wins on the 2048^2 r=32 dilation).
+template <int KA, int FBY, bool SINGLE, int LBN>
+__global__ void __launch_bounds__(kFB *FBY, LBN / (kFB * FBY)) k_fast_batched(const BatchVol *vols,
                                                                                const int2 *queue, int nq, int *next,
                                                                                const FastArgs A1) {
   extern __shared__ float2 sv_dyn[];
@@ -929,100 +930,69 @@ int fast_union_cap(double mean_segments_per_column) {
 }
 
 namespace {
-template <int KA>
-void *batched_kernel(int fby) {
-  switch (fby) {
-    case 1:
-      return reinterpret_cast<void *>(&k_fast_batched<KA, 1, false>);
-    case 2:
-      return reinterpret_cast<void *>(&k_fast_batched<KA, 2, false>);
-    case 4:
-      return reinterpret_cast<void *>(&k_fast_batched<KA, 4, false>);
-    case 8:
-      return reinterpret_cast<void *>(&k_fast_batched<KA, 8, false>);
-  }
-  return nullptr;
-}
-template <int KA>
-void *batched_kernel_single(int fby) {
-  switch (fby) {
-    case 1:
-      return reinterpret_cast<void *>(&k_fast_batched<KA, 1, true>);
-    case 2:
-      return reinterpret_cast<void *>(&k_fast_batched<KA, 2, true>);
-    case 4:
-      return reinterpret_cast<void *>(&k_fast_batched<KA, 4, true>);
-    case 8:
-      return reinterpret_cast<void *>(&k_fast_batched<KA, 8, true>);
-  }
-  return nullptr;
-}
-void *batched_kernel(int ka, int fby, bool single) {
-  if (single)
-    return ka == 64 ? batched_kernel_single<64>(fby)
-                    : ka == 32 ? batched_kernel_single<32>(fby) : ka == 24 ? batched_kernel_single<24>(fby) : nullptr;
-  return ka == 64 ? batched_kernel<64>(fby) : ka == 32 ? batched_kernel<32>(fby) : ka == 24 ? batched_kernel<24>(fby) : nullptr;
-}
+using BatchedFn = void (*)(const BatchVol *, const int2 *, int, int *, const FastArgs);
 
-template <int KA, bool SINGLE>
-void launch_batched(int fby, int grid, size_t smem, cudaStream_t st, const BatchVol *vols, const int2 *queue, int nq,
-                    int *next, const FastArgs &a1) {
-  const dim3 blk(kFB, fby);
+template <int KA, int FBY, bool SINGLE>
+BatchedFn batched_fn_regs(int regs) {
+  return regs == 64 ? &k_fast_batched<KA, FBY, SINGLE, 1024> : &k_fast_batched<KA, FBY, SINGLE, 768>;
+}
+template <int KA, int FBY>
+BatchedFn batched_fn_single(bool single, int regs) {
+  return single ? batched_fn_regs<KA, FBY, true>(regs) : batched_fn_regs<KA, FBY, false>(regs);
+}
+template <int KA>
+BatchedFn batched_fn_fby(int fby, bool single, int regs) {
   switch (fby) {
     case 1:
-      k_fast_batched<KA, 1, SINGLE><<<grid, blk, smem, st>>>(vols, queue, nq, next, a1);
-      break;
+      return batched_fn_single<KA, 1>(single, regs);
     case 2:
-      k_fast_batched<KA, 2, SINGLE><<<grid, blk, smem, st>>>(vols, queue, nq, next, a1);
-      break;
+      return batched_fn_single<KA, 2>(single, regs);
     case 4:
-      k_fast_batched<KA, 4, SINGLE><<<grid, blk, smem, st>>>(vols, queue, nq, next, a1);
-      break;
-    default:
-      k_fast_batched<KA, 8, SINGLE><<<grid, blk, smem, st>>>(vols, queue, nq, next, a1);
+      return batched_fn_single<KA, 4>(single, regs);
   }
+  return nullptr;
+}
+BatchedFn batched_fn(int ka, int fby, bool single, int regs) {
+  if (regs != 64 && regs != 80) return nullptr;
+  switch (ka) {
+    case 24:
+      return batched_fn_fby<24>(fby, single, regs);
+    case 32:
+      return batched_fn_fby<32>(fby, single, regs);
+    case 64:
+      return batched_fn_fby<64>(fby, single, regs);
+  }
+  return nullptr;
 }
 }  // namespace
 
-int fast_batched_blocks_per_sm(int ka, int fby, bool single) {
-  void *f = batched_kernel(ka, fby, single);
+int fast_batched_blocks_per_sm(int ka, int fby, bool single, int regs) {
+  const BatchedFn f = batched_fn(ka, fby, single, regs);
   if (!f) return 0;
   const size_t smem = sizeof(float2) * ka * kFB * fby;
   if (smem > 227 * 1024 ||
-      cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+      cudaFuncSetAttribute(reinterpret_cast<const void *>(f), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, kFB * fby, smem) != cudaSuccess) {
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, reinterpret_cast<const void *>(f), kFB * fby, smem) !=
+      cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
   return per_sm;
 }
 
-int fast_batched_launch(int ka, int fby, int grid, cudaStream_t st, const BatchVol *vols, const int2 *queue, int nq,
-                        int *next, const FastArgs *single) {
-  if ((ka != 24 && ka != 32 && ka != 64) || (fby != 1 && fby != 2 && fby != 4 && fby != 8)) return VO_EINVAL;
+int fast_batched_launch(int ka, int fby, int regs, int grid, cudaStream_t st, const BatchVol *vols,
+                        const int2 *queue, int nq, int *next, const FastArgs *single) {
+  const BatchedFn f = batched_fn(ka, fby, single != nullptr, regs);
+  if (!f) return VO_EINVAL;
   const size_t smem = sizeof(float2) * ka * kFB * fby;
   FastArgs none;
   std::memset(&none, 0, sizeof none);
-  const FastArgs &a1 = single ? *single : none;
-  if (single) {
-    if (ka == 64)
-      launch_batched<64, true>(fby, grid, smem, st, vols, queue, nq, next, a1);
-    else if (ka == 32)
-      launch_batched<32, true>(fby, grid, smem, st, vols, queue, nq, next, a1);
-    else
-      launch_batched<24, true>(fby, grid, smem, st, vols, queue, nq, next, a1);
-  } else {
-    if (ka == 64)
-      launch_batched<64, false>(fby, grid, smem, st, vols, queue, nq, next, a1);
-    else if (ka == 32)
-      launch_batched<32, false>(fby, grid, smem, st, vols, queue, nq, next, a1);
-    else
-      launch_batched<24, false>(fby, grid, smem, st, vols, queue, nq, next, a1);
-  }
+  f<<<grid, dim3(kFB, fby), smem, st>>>(vols, queue, nq, next, single ? *single : none);
   return VO_OK;
 }
 

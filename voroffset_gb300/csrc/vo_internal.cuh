@@ -221,14 +221,14 @@ void fast_pair_records(cudaStream_t st, const int2 *pairs, int npairs, const Dev
 // Union capacity (24, 32 or 64) of the main FP32 kernels for inputs with the
 // given mean segment count per column.
 int fast_union_cap(double mean_segments_per_column);
-// Launch of the persistent kernel with union capacity ka (24, 32 or 64) and `fby`
-// rows of kFastCols columns per block (fby in {1, 2, 4, 8});
-// fast_batched_blocks_per_sm is the occupancy of that shape (0: unusable).
-// single: the round's one dilation's arguments (passed as a kernel
-// parameter), or nullptr for a round of several dilations.
-int fast_batched_launch(int ka, int fby, int grid, cudaStream_t st, const BatchVol *vols, const int2 *queue, int nq,
-                        int *next, const FastArgs *single);
-int fast_batched_blocks_per_sm(int ka, int fby, bool single);
+// Launch of the batch kernel with union capacity ka (24, 32 or 64), `fby`
+// rows of kFastCols columns per block (1, 2 or 4) and a register budget of
+// regs (64 or 80) per thread; fast_batched_blocks_per_sm is the occupancy of
+// that variant (0: unusable). single: the round's one dilation's arguments
+// (passed as a kernel parameter), or nullptr for a round of several.
+int fast_batched_launch(int ka, int fby, int regs, int grid, cudaStream_t st, const BatchVol *vols,
+                        const int2 *queue, int nq, int *next, const FastArgs *single);
+int fast_batched_blocks_per_sm(int ka, int fby, bool single, int regs);
 // Second tier of a batch round over the dilations vols[0..nv) (grid-stride).
 void fast_batched_mid_launch(cudaStream_t st, const BatchVol *vols, int nv, int grid);
 // Third tier (FP64) of a batch round; scratch holds
