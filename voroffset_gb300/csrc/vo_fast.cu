@@ -511,14 +511,15 @@ __global__ void k_dh_tables(int Dy, int W, const double *__restrict__ H, const i
 // Dominance widths, one thread per column. For segment i and direction k
 // (neighbour (x-1, y), (x+1, y), (x, y-1), (x, y+1)):
 //   w_i = min over the neighbour's segments j of max(z1_j - z1_i, z2_i - z2_j),
-// every difference rounded up (so w bounds the exact value from above; +inf
-// outside the grid or without a neighbour segment). The scan stops after the
+// evaluated in FP32 on bounds of the FP64 values with every difference
+// rounded up, so w bounds the exact value from above (+inf outside the grid
+// or without a neighbour segment). The scan stops after the
 // first neighbour segment starting above segment i: every later neighbour
 // segment gives a larger value. The column's width per direction is the max
 // over its segments (-inf for an empty column), stored as FP16 rounded up in
 // the column record col[c] = (beg, end, x- | x+ << 16, y- | y+ << 16).
 __global__ void k_dominance(int nx, int ny, const int32_t *__restrict__ beg, const int32_t *__restrict__ end,
-                            const double2 *__restrict__ z, int4 *__restrict__ col, unsigned *__restrict__ dmask) {
+                            const float2 *__restrict__ zf, int4 *__restrict__ col, unsigned *__restrict__ dmask) {
   const int ncols = nx * ny;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncols) return;
@@ -532,35 +533,37 @@ __global__ void k_dominance(int nx, int ny, const int32_t *__restrict__ beg, con
     nb0[k] = in ? beg[cn] : 0;
     nb1[k] = in ? end[cn] : 0;
   }
-  double cmax[4] = {-INFINITY, -INFINITY, -INFINITY, -INFINITY};
+  float cmax[4] = {-INFINITY, -INFINITY, -INFINITY, -INFINITY};
   unsigned bits[4][kDomLevels];
   for (int k = 0; k < 4; ++k)
     for (int l = 0; l < kDomLevels; ++l) bits[k][l] = 0u;
   const bool masked = k1 - k0 <= 32;
   for (int i = k0; i < k1; ++i) {
-    const double2 si = z[i];
+    // bounds of the exact values: an FP32 copy is within half an ulp of its
+    // FP64 value, so the neighbouring floats enclose it
+    const float2 fi = zf[i];
+    const float i1 = nextafterf(fi.x, -INFINITY), i2 = nextafterf(fi.y, INFINITY);
     for (int k = 0; k < 4; ++k) {
-      double best = INFINITY;
+      float best = INFINITY;
       for (int j = nb0[k]; j < nb1[k]; ++j) {
-        const double2 sj = z[j];
-        const double lo = __dsub_ru(sj.x, si.x), hi = __dsub_ru(si.y, sj.y);
-        const double m = lo > hi ? lo : hi;
+        const float2 fj = zf[j];
+        const float lo = __fsub_ru(nextafterf(fj.x, INFINITY), i1);
+        const float hi = __fsub_ru(i2, nextafterf(fj.y, -INFINITY));
+        const float m = lo > hi ? lo : hi;
         best = m < best ? m : best;
-        if (sj.x > si.y) break;
+        if (fj.x > fi.y) break;  // any early stop only leaves the bound larger
       }
       cmax[k] = best > cmax[k] ? best : cmax[k];
-      if (masked) {
-        const float w = __double2float_ru(best);
+      if (masked)
         for (int l = 0; l < kDomLevels; ++l)
-          if (w <= dom_level(l)) bits[k][l] |= 1u << (i - k0);
-      }
+          if (best <= dom_level(l)) bits[k][l] |= 1u << (i - k0);
     }
   }
   if (dmask)
     for (int k = 0; k < 4; ++k)
       for (int l = 0; l < kDomLevels; ++l) dmask[(size_t)(k * kDomLevels + l) * ncols + c] = bits[k][l];
   unsigned h[4];
-  for (int k = 0; k < 4; ++k) h[k] = __half_as_ushort(__float2half_ru(__double2float_ru(cmax[k])));
+  for (int k = 0; k < 4; ++k) h[k] = __half_as_ushort(__float2half_ru(cmax[k]));
   col[c] = make_int4(k0, k1, (int)(h[0] | (h[1] << 16)), (int)(h[2] | (h[3] << 16)));
 }
 
@@ -912,7 +915,8 @@ void fast_prepare(cudaStream_t st, int nx, int ny, const int32_t *beg, const int
   cudaMemsetAsync(maxbits, 0, sizeof(unsigned int), st);
   k_to_f32_cols<<<(ncols + 255) / 256, 256, 0, st>>>(ncols, beg, end, (const double *)z, zf, maxbits);
   k_guard<<<1, 1, 0, st>>>(maxbits, R, E);
-  k_dominance<<<(ncols + 127) / 128, 128, 0, st>>>(nx, ny, beg, end, z, col, dmask);
+  k_dominance<<<(ncols + 127) / 128, 128, 0, st>>>(nx, ny, beg, end, reinterpret_cast<const float2 *>(zf), col,
+                                                    dmask);
 }
 
 void fast_pair_records(cudaStream_t st, const int2 *pairs, int npairs, const DeviceTables &T, float4 *prec) {
