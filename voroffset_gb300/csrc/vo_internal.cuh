@@ -149,12 +149,9 @@ struct SlotVol {
 int slot_alloc(vo_ctx *ctx, const vo_grid &g, int cap, SlotVol &v);
 void slot_free(vo_ctx *ctx, SlotVol &v);
 SlotVol slot_view(const vo_volume *in, int cap);
-void slot_end_from_counts(vo_ctx *ctx, SlotVol &v, const int32_t *counts);
-int slot_negate(vo_ctx *ctx, const SlotVol &in, SlotVol &out, int *overflow);
-int slot_normalize(vo_ctx *ctx, const SlotVol &in, SlotVol &out, int *overflow);
-int slot_negate_inv(vo_ctx *ctx, const SlotVol &in, const vo_grid &g, SlotVol &out, int *overflow);
-// The same three steps as launches only, into already allocated outputs
-// (for graph capture).
+// Complement with a one-column border (negate), normalisation of inverted
+// pairs, and complement back on the inner range (negate_inv), as launches into
+// already allocated slot outputs (batch plans record them for graph capture).
 void slot_negate_launch(cudaStream_t st, const SlotVol &in, const SlotVol &out, int *overflow);
 void slot_normalize_launch(cudaStream_t st, const SlotVol &in, const SlotVol &out, int *overflow);
 void slot_negate_inv_launch(cudaStream_t st, const SlotVol &in, const vo_grid &g, const SlotVol &out,

@@ -801,10 +801,6 @@ __global__ void k_slot_beg(int ncols, int cap, int32_t *beg) {
   if (c < ncols) beg[c] = c * cap;
 }
 
-__global__ void k_slot_end_from_counts(int ncols, int cap, const int32_t *counts, int32_t *end) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c < ncols) end[c] = c * cap + counts[c];
-}
 
 // negate (Voronoi.cpp:18-55) into a grown (nx+2) x (ny+2) slot volume.
 __global__ void k_negate_slot(int nx, int ny, const int32_t *__restrict__ beg, const int32_t *__restrict__ end,
@@ -1272,12 +1268,6 @@ SlotVol slot_view(const vo_volume *in, int cap) {
   return v;
 }
 
-void slot_end_from_counts(vo_ctx *ctx, SlotVol &v, const int32_t *counts) {
-  const int ncols = v.grid.nx * v.grid.ny;
-  k_slot_end_from_counts<<<nblocks(ncols, 256), 256, 0, ctx->stream>>>(ncols, v.cap, counts, v.end);
-  ctx->launches += 1;
-}
-
 void slot_negate_launch(cudaStream_t st, const SlotVol &in, const SlotVol &out, int *overflow) {
   const vo_grid &g = in.grid;
   const double zmin = g.origin[2] / g.spacing - 1;
@@ -1286,28 +1276,9 @@ void slot_negate_launch(cudaStream_t st, const SlotVol &in, const SlotVol &out, 
       g.nx, g.ny, in.beg, in.end, in.z, zmin, zmax, out.cap, out.end, out.z, overflow);
 }
 
-int slot_negate(vo_ctx *ctx, const SlotVol &in, SlotVol &out, int *overflow) {
-  vo_grid g2 = in.grid;
-  g2.nx += 2;
-  g2.ny += 2;
-  int rc = slot_alloc(ctx, g2, in.cap + 1, out);
-  if (rc) return rc;
-  slot_negate_launch(ctx->stream, in, out, overflow);
-  ctx->launches += 1;
-  return VO_OK;
-}
-
 void slot_normalize_launch(cudaStream_t st, const SlotVol &in, const SlotVol &out, int *overflow) {
   const int ncols = in.grid.nx * in.grid.ny;
   k_norm_slot<<<nblocks(ncols, 128), 128, 0, st>>>(ncols, in.beg, in.end, in.z, out.cap, out.end, out.z, overflow);
-}
-
-int slot_normalize(vo_ctx *ctx, const SlotVol &in, SlotVol &out, int *overflow) {
-  int rc = slot_alloc(ctx, in.grid, in.cap + 2, out);
-  if (rc) return rc;
-  slot_normalize_launch(ctx->stream, in, out, overflow);
-  ctx->launches += 1;
-  return VO_OK;
 }
 
 void slot_negate_inv_launch(cudaStream_t st, const SlotVol &in, const vo_grid &g, const SlotVol &out,
@@ -1316,14 +1287,6 @@ void slot_negate_inv_launch(cudaStream_t st, const SlotVol &in, const vo_grid &g
   const double zmax = g.origin[2] / g.spacing + 2 * g.padding + g.extent[2] / g.spacing + 1;
   k_negate_inv_slot<<<nblocks((int64_t)g.nx * g.ny, 256), 256, 0, st>>>(
       g.nx, g.ny, in.beg, in.end, in.z, zmin + 1, zmax - 1, out.cap, out.end, out.z, overflow);
-}
-
-int slot_negate_inv(vo_ctx *ctx, const SlotVol &in, const vo_grid &g, SlotVol &out, int *overflow) {
-  int rc = slot_alloc(ctx, g, in.cap + 1, out);
-  if (rc) return rc;
-  slot_negate_inv_launch(ctx->stream, in, g, out, overflow);
-  ctx->launches += 1;
-  return VO_OK;
 }
 
 int slot_max_count(vo_ctx *ctx, const SlotVol &v, int *d_max) {
