@@ -269,23 +269,25 @@ def batch_main(args, rank, world, local):
         for o in plan.outputs():
             o.free()
 
+    barrier, maxreduce = sync_helpers(world)
+
     def timed(f, steps, warmup):
         for _ in range(warmup):
             f()
-        torch.cuda.synchronize()
+        barrier()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(steps):
             f()
         e1.record(stream)
-        torch.cuda.synchronize()
-        return e0.elapsed_time(e1)
+        barrier()
+        return maxreduce(e0.elapsed_time(e1))
 
     clocks = ClockSampler(local)
     clocks.start()
     ms = timed(step, args.steps, args.warmup)
     clk = clocks.stop()
-    value = world * cols * args.steps / (ms / 1e3) / 1e6
+    value = job_rate(world, cols * args.steps, ms / 1e3)
     progress("batched steps timed")
 
     def loop_step():
@@ -294,7 +296,7 @@ def batch_main(args, rank, world, local):
             o.free()
 
     loop_ms = timed(loop_step, 1, 1)
-    arms = {"one_by_one_fast": {"value": world * cols / (loop_ms / 1e3) / 1e6, "unit": "Mcolumns/s",
+    arms = {"one_by_one_fast": {"value": job_rate(world, cols, loop_ms / 1e3), "unit": "Mcolumns/s",
                                 "ms_per_step": loop_ms}}
     arms["batched_vs_one_by_one"] = value / arms["one_by_one_fast"]["value"]
     st_run = plan.stats()
@@ -327,14 +329,47 @@ def batch_main(args, rank, world, local):
     return 0
 
 
+def sync_helpers(world: int, cuda: bool = True):
+    """barrier(): device sync, then a barrier over the ranks; maxreduce(x): the
+    largest x over the ranks (the job's time is its slowest rank's)."""
+    import torch
+
+    def barrier():
+        if cuda:
+            torch.cuda.synchronize()
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def maxreduce(x):
+        if world == 1:
+            return x
+        import torch.distributed as dist
+        t = torch.tensor([x], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    return barrier, maxreduce
+
+
+def job_rate(world: int, units_per_rank: float, seconds: float) -> float:
+    """Whole-job throughput in millions of units per second: every rank
+    processes units_per_rank in the (slowest rank's) time `seconds`."""
+    return world * units_per_rank / seconds / 1e6
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
-    if args.workload.startswith("batch") and args.impl != "reference":
-        return batch_main(args, rank, world, local)
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")
+    if args.workload.startswith("batch") and args.impl != "reference":
+        rc = batch_main(args, rank, world, local)
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return rc
     if args.impl == "reference":
         rc = reference_arm(args, rank, world)
         if world > 1:
@@ -352,19 +387,7 @@ def main():
     ctx = V.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
 
-    def barrier():
-        torch.cuda.synchronize()
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
-
-    def maxreduce(x):
-        if world == 1:
-            return x
-        import torch.distributed as dist
-        t = torch.tensor([x], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    barrier, maxreduce = sync_helpers(world)
 
     # ---------------- learned sizer (batched arms)
     sizer = None
@@ -425,7 +448,7 @@ def main():
     dev_ms = timed(step, args.steps, args.warmup)
     clk = clocks.stop()
     launches, kernel_total_ms, out_segs, mid = acc["launches"], acc["kernel_ms"], acc["out_segs"], acc["mid"]
-    value = world * ncols * args.steps / (dev_ms / 1e3) / 1e6
+    value = job_rate(world, ncols * args.steps, dev_ms / 1e3)
     # kernel time of the warm-up steps was accumulated too: keep the timed steps only
     kernel_ms = kernel_total_ms * args.steps / (args.steps + args.warmup)
     launches = launches * args.steps // (args.steps + args.warmup)
@@ -470,7 +493,7 @@ def main():
         d2h = e2e_step()
     barrier()
     e2e_s = maxreduce(time.perf_counter() - t0)
-    e2e = world * ncols * args.steps / e2e_s / 1e6
+    e2e = job_rate(world, ncols * args.steps, e2e_s)
 
     # ---------------- roofline of the dominant kernel
     kname = {"batched": "k_fast_batched", "fast": "k_fast", "separable": "k_pass2", "brute": "k_brute"}[args.method]
