@@ -227,3 +227,48 @@ def test_gpu_inverted_pairs_normalised(ctx, vo, oracle, method):
         want = oracle.morph(ogrid(oracle, grid), offs, z, r, "dilation", "brute" if method == "brute" else "separable")
         got, _ = run(ctx, grid, offs, z, "dilation", r, method)
         assert_same(got, want, tol=0.0, what=f"{method} r={r}")
+
+
+@pytest.mark.parametrize("shift", [-3.0e5, 7.5e5])
+def test_gpu_fast_far_from_origin(ctx, vo, oracle, shift):
+    """z values of magnitude ~1e5-1e6 leave FP32 about 0.06 dexel of precision:
+    most merge decisions fall inside the guard band and are taken in FP64, and
+    the result stays bit-identical (both methods, all ops)."""
+    grid, offs, z = vo.synth_volume(vo.SynthSpec(40, n_spheres=12, s_rmin=2, s_rmax=9, n_cyl=3, seed=17))
+    z = z + shift
+    g = vo.Grid(grid.nx, grid.ny, (0.0, 0.0, shift), grid.extent, grid.spacing, grid.padding)
+    for op in ("dilation", "erosion", "closing"):
+        want = oracle.morph(ogrid(oracle, g), offs, z, 5.5, op)
+        got, _ = run(ctx, g, offs, z, op, 5.5, "fast")
+        assert_same(got, want, tol=0.0, what=f"{op} shift={shift}")
+
+
+def test_gpu_fast_largest_radius(ctx, vo, oracle):
+    """r = 255 (the largest radius; ~51,000 (|dx|, |dy|) pairs) on a small grid."""
+    grid, offs, z = vo.synth_volume(vo.SynthSpec(48, n_spheres=10, s_rmin=2, s_rmax=8, seed=23))
+    want = oracle.morph(ogrid(oracle, grid), offs, z, 255.0, "dilation")
+    got, _ = run(ctx, grid, offs, z, "dilation", 255.0, "fast")
+    assert_same(got, want, tol=0.0)
+    outs, _ = ctx.morph_batched([ctx.upload(grid, offs, z)], ["dilation"], [255.0], "fast")
+    assert_same(ctx.download(outs[0]), want, tol=0.0, what="batch plan")
+
+
+@pytest.mark.parametrize("shape", [(1, 200), (200, 1), (3, 97)])
+def test_gpu_fast_thin_grids_batch(ctx, vo, oracle, shape):
+    """Grids one or a few columns wide, through a batch plan with every op."""
+    nx, ny = shape
+    rng = np.random.default_rng(nx * 1000 + ny)
+    cols = []
+    for _ in range(nx * ny):
+        k = int(rng.integers(0, 4))
+        v = np.sort(rng.uniform(0, 60, 2 * k))
+        cols.append(v)
+    offs = np.zeros(nx * ny + 1, np.int32)
+    offs[1:] = np.cumsum([c.size // 2 for c in cols])
+    z = np.concatenate(cols) if offs[-1] else np.zeros(0)
+    g = vo.Grid(nx, ny, (0, 0, 0), (nx, ny, 60), 1.0, 0)
+    v = ctx.upload(g, offs, z)
+    ops = ["dilation", "erosion", "opening", "closing"]
+    outs, _ = ctx.morph_batched([v] * 4, ops, [3.5] * 4, "fast")
+    for op, out in zip(ops, outs):
+        assert_same(ctx.download(out), oracle.morph(ogrid(oracle, g), offs, z, 3.5, op), tol=0.0, what=op)
