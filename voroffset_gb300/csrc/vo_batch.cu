@@ -309,8 +309,8 @@ int tune_shape(vo_ctx *ctx, vo_batch *b, const std::vector<DilPlan> &dils, const
       *regs_out = (kv.second >> 17) & 1 ? 80 : 64;
       return VO_OK;
     }
-  // union capacities to try: 64 for dense inputs, else 24 and 32
-  std::vector<int> kas = ka_hint == 64 ? std::vector<int>{64} : std::vector<int>{24, 32};
+  // union capacities to try: 48 and 64 for dense inputs, else 24 and 32
+  std::vector<int> kas = ka_hint == 64 ? std::vector<int>{48, 64} : std::vector<int>{24, 32};
   int best_ka = kas.back(), best_pers = 1, best_regs = 64;
   const int sms = sm_count();
   int best = 4;

@@ -963,6 +963,8 @@ BatchedFn batched_fn(int ka, int fby, bool single, int regs) {
       return batched_fn_fby<24>(fby, single, regs);
     case 32:
       return batched_fn_fby<32>(fby, single, regs);
+    case 48:
+      return batched_fn_fby<48>(fby, single, regs);
     case 64:
       return batched_fn_fby<64>(fby, single, regs);
   }
