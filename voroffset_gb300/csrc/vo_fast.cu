@@ -816,8 +816,11 @@ int dilate_fast(vo_ctx *ctx, double R, const vo_volume *in, vo_volume **out, vo_
   FastArgs A{nx, ny, h.W, in->offs, in->offs + 1, (const double *)in->z, zf, T->Hf, T->H, dpairs,
              (int)pairs.size(), dE, col, prec, dmask};
   const dim3 blk(kFB, kFBY), grd((nx + kFB - 1) / kFB, (ny + kFBY - 1) / kFBY);
-  // union capacity from the input's mean segment count per column (24, 32 or 64)
-  const int ka = fast_union_cap((double)in->nseg / std::max(ncols, 1));
+  // union capacity from the input's mean segment count per column (24, 32,
+  // 48 or 64; dense inputs take 48 up to 24 segments per column, which keeps
+  // more warps per SM than 64, the rest going to the second tier)
+  const double mean_segs = (double)in->nseg / std::max(ncols, 1);
+  const int ka = fast_union_cap(mean_segs) == 64 ? (mean_segs > 24.0 ? 64 : 48) : fast_union_cap(mean_segs);
   const size_t smem = sizeof(float2) * ka * kFB * kFBY;
   double2 *staging = nullptr;
   if (!rc) rc = dalloc(ctx, &staging, (size_t)ncols * ka);
@@ -829,6 +832,8 @@ int dilate_fast(vo_ctx *ctx, double R, const vo_volume *in, vo_volume **out, vo_
     cudaEventRecord(ctx->ev[4], ctx->stream);
     if (ka == 64)
       k_fast<64><<<grd, blk, smem, ctx->stream>>>(A, counts, staging, ctx->d_flags, ovf_cols);
+    else if (ka == 48)
+      k_fast<48><<<grd, blk, smem, ctx->stream>>>(A, counts, staging, ctx->d_flags, ovf_cols);
     else if (ka == 32)
       k_fast<32><<<grd, blk, smem, ctx->stream>>>(A, counts, staging, ctx->d_flags, ovf_cols);
     else
