@@ -91,6 +91,11 @@ __device__ __noinline__ bool ex_u_lt_u(const FastArgs &A, const UnionIds<KA> &U,
   return a < b;
 }
 
+// The FP16 in the low (lo != 0) or high half of v.
+__device__ __forceinline__ __half half_of(unsigned v, int lo) {
+  return __ushort_as_half((unsigned short)(lo ? (v & 0xffffu) : (v >> 16)));
+}
+
 // The FP16 in the low (lo != 0) or high half of v, as a float.
 __device__ __forceinline__ float half_lo_hi(unsigned v, int lo) {
   return __half2float(__ushort_as_half((unsigned short)(lo ? (v & 0xffffu) : (v >> 16))));
@@ -161,11 +166,13 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
     // source column dominated in either direction is skipped whole; of the
     // others (up to 32 segments), the segments dominated at the pair's levels
     const float dhx = pc.z, dhy = pc.w;
+    // FP16 bounds of the pair's growths (rounded down) for the source tests
+    const __half dhx_h = __float2half_rd(dhx), dhy_h = __float2half_rd(dhy);
     // Per source: [kb, ke) and the mask of its kept segments (bit j: segment
     // kb + j); a source of more than 32 segments keeps all (m = 0, dense).
 #define SRC(S, C, DM, KB, KE, M)                                                                        \
   {                                                                                                     \
-    const bool dom = half_lo_hi((unsigned)(C).z, (S) & 1) <= dhx || half_lo_hi((unsigned)(C).w, (S) & 2) <= dhy; \
+    const bool dom = __hle(half_of((unsigned)(C).z, (S) & 1), dhx_h) || __hle(half_of((unsigned)(C).w, (S) & 2), dhy_h); \
     KB = dom ? 0 : (C).x;                                                                               \
     KE = dom ? 0 : (C).y;                                                                               \
     const int ns_ = KE - KB;                                                                            \
@@ -233,6 +240,15 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
           const float lo = zf.x - h, hi = zf.y + h;
           const int il = 2 * k, ih = 2 * k + 1;
           // skip union intervals that end strictly below the candidate: U.hi[cur] < lo
+          // (the next interval's values are loaded one step ahead)
+          if (cur < n && lo - cv.y > E) {
+            float2 cn = cur + 1 < n ? SV(cur + 1) : cv;
+            do {
+              ++cur;
+              cv = cn;
+              if (cur + 1 < n) cn = SV(cur + 1);
+            } while (cur < n && lo - cv.y > E);
+          }
           while (cur < n && GUARD(lo - cv.y, E, ex_u_lt_c(A, U, cur, true, il, da, false))) {
             ++cur;
             if (cur < n) cv = SV(cur);
