@@ -58,8 +58,8 @@ constexpr int kMidThreads = 32;
 // FP32 comparison falls inside the guard band or the output is written.
 template <int KA>
 struct UnionIds {
-  int li[KA], hi_i[KA];  // input value index of the lower / upper endpoint
-  int lda[KA], hda[KA];  // d | a << 8 of the lower / upper endpoint
+  // (input value index, d | a << 8) of the lower / upper endpoint
+  int2 lo[KA], hi[KA];
 };
 
 __device__ __forceinline__ double exact_val(const FastArgs &A, int idx, int da, bool plus) {
@@ -73,21 +73,21 @@ __device__ __forceinline__ double exact_val(const FastArgs &A, int idx, int da, 
 template <int KA>
 __device__ __noinline__ bool ex_u_lt_c(const FastArgs &A, const UnionIds<KA> &U, int j, bool jhi, int idx, int da,
                                        bool plus) {
-  const double u = jhi ? exact_val(A, U.hi_i[j], U.hda[j], true) : exact_val(A, U.li[j], U.lda[j], false);
+  const double u = jhi ? exact_val(A, U.hi[j].x, U.hi[j].y, true) : exact_val(A, U.lo[j].x, U.lo[j].y, false);
   return u < exact_val(A, idx, da, plus);
 }
 // Candidate endpoint < union endpoint?
 template <int KA>
 __device__ __noinline__ bool ex_c_lt_u(const FastArgs &A, const UnionIds<KA> &U, int idx, int da, bool plus, int j,
                                        bool jhi) {
-  const double u = jhi ? exact_val(A, U.hi_i[j], U.hda[j], true) : exact_val(A, U.li[j], U.lda[j], false);
+  const double u = jhi ? exact_val(A, U.hi[j].x, U.hi[j].y, true) : exact_val(A, U.lo[j].x, U.lo[j].y, false);
   return exact_val(A, idx, da, plus) < u;
 }
 // Union endpoint (i, ihi) < union endpoint (j, jhi)?
 template <int KA>
 __device__ __noinline__ bool ex_u_lt_u(const FastArgs &A, const UnionIds<KA> &U, int i, bool ihi, int j, bool jhi) {
-  const double a = ihi ? exact_val(A, U.hi_i[i], U.hda[i], true) : exact_val(A, U.li[i], U.lda[i], false);
-  const double b = jhi ? exact_val(A, U.hi_i[j], U.hda[j], true) : exact_val(A, U.li[j], U.lda[j], false);
+  const double a = ihi ? exact_val(A, U.hi[i].x, U.hi[i].y, true) : exact_val(A, U.lo[i].x, U.lo[i].y, false);
+  const double b = jhi ? exact_val(A, U.hi[j].x, U.hi[j].y, true) : exact_val(A, U.lo[j].x, U.lo[j].y, false);
   return a < b;
 }
 
@@ -270,30 +270,24 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
               } else {
                 for (int j = n; j > cur; --j) {
                   SV(j) = SV(j - 1);
-                  U.li[j] = U.li[j - 1];
-                  U.hi_i[j] = U.hi_i[j - 1];
-                  U.lda[j] = U.lda[j - 1];
-                  U.hda[j] = U.hda[j - 1];
+                  U.lo[j] = U.lo[j - 1];
+                  U.hi[j] = U.hi[j - 1];
                 }
                 cv = make_float2(lo, hi);
                 SV(cur) = cv;
-                U.li[cur] = il;
-                U.hi_i[cur] = ih;
-                U.lda[cur] = da;
-                U.hda[cur] = da;
+                U.lo[cur] = make_int2(il, da);
+                U.hi[cur] = make_int2(ih, da);
                 ++n;
               }
             } else {
               // overlapping or touching U[cur]: extend it
               if (GUARD(cv.x - lo, E, ex_c_lt_u(A, U, il, da, false, cur, false))) {
                 cv.x = lo;
-                U.li[cur] = il;
-                U.lda[cur] = da;
+                U.lo[cur] = make_int2(il, da);
               }
               if (GUARD(hi - cv.y, E, ex_u_lt_c(A, U, cur, true, ih, da, true))) {
                 cv.y = hi;
-                U.hi_i[cur] = ih;
-                U.hda[cur] = da;
+                U.hi[cur] = make_int2(ih, da);
                 // absorb following intervals that now start at or below the new end
                 int j = cur + 1;
                 while (j < n) {
@@ -301,8 +295,7 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
                   if (GUARD(nv.x - cv.y, E, ex_u_lt_u(A, U, cur, true, j, false))) break;  // U.hi[cur] < U.lo[j]
                   if (GUARD(nv.y - cv.y, E, ex_u_lt_u(A, U, cur, true, j, true))) {       // U.hi[cur] < U.hi[j]
                     cv.y = nv.y;
-                    U.hi_i[cur] = U.hi_i[j];
-                    U.hda[cur] = U.hda[j];
+                    U.hi[cur] = U.hi[j];
                   }
                   ++j;
                 }
@@ -310,10 +303,8 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
                 if (gone > 0) {
                   for (int m = cur + 1; m + gone < n; ++m) {
                     SV(m) = SV(m + gone);
-                    U.li[m] = U.li[m + gone];
-                    U.hi_i[m] = U.hi_i[m + gone];
-                    U.lda[m] = U.lda[m + gone];
-                    U.hda[m] = U.hda[m + gone];
+                    U.lo[m] = U.lo[m + gone];
+                    U.hi[m] = U.hi[m + gone];
                   }
                   n -= gone;
                 }
@@ -337,7 +328,7 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
 template <int KA>
 __device__ __forceinline__ void write_union(const FastArgs &A, const UnionIds<KA> &U, int n, double2 *out) {
   for (int k = 0; k < n; ++k)
-    out[k] = make_double2(exact_val(A, U.li[k], U.lda[k], false), exact_val(A, U.hi_i[k], U.hda[k], true));
+    out[k] = make_double2(exact_val(A, U.lo[k].x, U.lo[k].y, false), exact_val(A, U.hi[k].x, U.hi[k].y, true));
 }
 
 // One pass: the exact union of every output column goes to its fixed-capacity
