@@ -103,13 +103,26 @@ def test_pruned_union_equals_oracle(vo, oracle, R, seed):
     assert kept < total  # the rule prunes something on these shapes
 
 
-LEVELS = [0.0, 1 / 16, 1 / 8, 1 / 4, 1 / 2, 1.0, 2.0, 4.0]
+NLEVELS = 15
 
 
-def _level(dh):
+def _levels(H):
+    """Dominance level thresholds of a radius, as the library's table builder
+    sets them: 0, then the growths of H over one lattice step (FP32 lower
+    bounds) at quantiles (l - 1/2) / 14 of their sorted list."""
+    g = sorted([_down(H[(d, a - 1)] - H[(d, a)]) for (d, a) in H if a >= 1] +
+               [_down(H[(d - 1, a)] - H[(d, a)]) for (d, a) in H if d >= 1])
+    t = [0.0]
+    for lv in range(1, NLEVELS):
+        v = g[int(math.floor((lv - 0.5) / (NLEVELS - 1) * (len(g) - 1) + 0.5))] if g else 0.0
+        t.append(max(v, 0.0))
+    return t
+
+
+def _level(dh, levels):
     """Largest level <= dh (-1: none), as the kernels quantise a pair's growth of H."""
     lv = -1
-    for i, t in enumerate(LEVELS):
+    for i, t in enumerate(levels):
         if t <= dh:
             lv = i
     return lv
@@ -143,8 +156,9 @@ def test_segment_masks_by_level_equal_oracle(vo, oracle, R, seed):
     cols = [list(map(tuple, z[2 * offs[c]:2 * offs[c + 1]].reshape(-1, 2))) for c in range(g.ncols)]
     Dy, Dx, H = _tables(R)
     sw = _segment_widths(nx, ny, cols)
-    lx = {(d, a): _level(_down(H[(d, a - 1)] - H[(d, a)])) if a >= 1 else -1 for (d, a) in H}
-    ly = {(d, a): _level(_down(H[(d - 1, a)] - H[(d, a)])) if d >= 1 else -1 for (d, a) in H}
+    LEVELS = _levels(H)
+    lx = {(d, a): _level(_down(H[(d, a - 1)] - H[(d, a)]), LEVELS) if a >= 1 else -1 for (d, a) in H}
+    ly = {(d, a): _level(_down(H[(d - 1, a)] - H[(d, a)]), LEVELS) if d >= 1 else -1 for (d, a) in H}
     kept = total = 0
     wo, wz = oracle.morph(ogrid(oracle, g), offs, z, R, "dilation")
     for c in range(nx * ny):

@@ -2,6 +2,7 @@
 // volumes, radius tables and operation chaining. The kernels live in
 // vo_morph.cu (morphology), vo_dexel.cu (ray rasterisation) and vo_reduce.cu
 // (xor volume).
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -25,6 +26,43 @@ int cuda_error(vo_ctx *ctx, cudaError_t e, const char *where) {
 
 void dfree(vo_ctx *ctx, void *p) {
   if (p) cudaFreeAsync(p, ctx->stream);
+}
+
+// FP32 lower bound of a - b as the device computes it
+// (__double2float_rd(__dsub_rd(a, b))): the FP64 difference rounded to
+// nearest is moved down one ulp when its TwoSum error is negative, then the
+// FP32 conversion rounded to nearest is moved down when it lies above.
+static float sub_rd_f32(double a, double b) {
+  const double c = -b, s = a + c, bb = s - a;
+  const double e = (a - (s - bb)) + (c - bb);
+  const double sd = e < 0.0 ? std::nextafter(s, -INFINITY) : s;
+  float f = (float)sd;
+  if ((double)f > sd) f = std::nextafterf(f, -INFINITY);
+  return f;
+}
+
+// Dominance level thresholds for the tables' radius: t[0] = 0 and t[l] for
+// l >= 1 the value at quantile (l - 1/2) / (kDomLevels - 1) of the sorted
+// growths of H over one lattice step (x steps for a >= 1, y steps for
+// d >= 1), each as the FP32 lower bound the device's pair records hold.
+static void dom_levels(Tables &t) {
+  std::vector<float> g;
+  for (int d = 0; d <= t.Dy; ++d)
+    for (int a = 0; a <= t.Dx[d]; ++a) {
+      const double h = t.H[(size_t)d * t.W + a];
+      if (a >= 1) g.push_back(sub_rd_f32(t.H[(size_t)d * t.W + a - 1], h));
+      if (d >= 1) g.push_back(sub_rd_f32(t.H[(size_t)(d - 1) * t.W + a], h));
+    }
+  std::sort(g.begin(), g.end());
+  t.dom.t[0] = 0.f;
+  for (int l = 1; l < kDomLevels; ++l) {
+    float v = 0.f;
+    if (!g.empty()) {
+      const double q = ((double)l - 0.5) / (double)(kDomLevels - 1);
+      v = g[(size_t)std::floor(q * (double)(g.size() - 1) + 0.5)];
+    }
+    t.dom.t[l] = v > 0.f ? v : 0.f;
+  }
 }
 
 // Host tables with the reference's expressions (compiled with
@@ -69,6 +107,7 @@ int build_tables(double R, int kmax, Tables &t) {
       const double fx = (double)dx * dx, fy = (double)dy * dy;
       if (fx + fy <= R * R) t.HB[(size_t)dy * (Dy + 1) + dx] = std::sqrt(R * R - fx - fy);
     }
+  dom_levels(t);
   return VO_OK;
 }
 

@@ -416,8 +416,9 @@ int plan_dilation_round(vo_ctx *ctx, vo_batch *b, std::vector<DilPlan> &dils, bo
     unsigned *dmask = d.dmask;
     unsigned int *mb = d.maxbits;
     const float R = (float)b->radii[d.vol];
-    record(b, 3, [in, zf, E, mb, R, col, dmask](cudaStream_t st) {
-      fast_prepare(st, in.grid.nx, in.grid.ny, in.beg, in.end, in.z, zf, mb, R, E, col, dmask);
+    const DomLevels L = d.T->host.dom;
+    record(b, 3, [in, zf, E, mb, R, col, dmask, L](cudaStream_t st) {
+      fast_prepare(st, in.grid.nx, in.grid.ny, in.beg, in.end, in.z, zf, mb, R, E, col, dmask, L);
     });
     // candidates per column ~ 4 x pairs x mean segments of the input (no sizer)
     const double segs = d.in.cap > 0 && d.in.owns ? d.in.cap * 0.5 : (double)d.in.entries / std::max(ncols, 1);

@@ -101,9 +101,6 @@ __device__ __forceinline__ float half_lo_hi(unsigned v, int lo) {
   return __half2float(__ushort_as_half((unsigned short)(lo ? (v & 0xffffu) : (v >> 16))));
 }
 
-// Dominance level thresholds: 0, 1/16, 1/8, 1/4, 1/2, 1, 2, 4 (exact in FP32).
-__device__ __forceinline__ float dom_level(int l) { return l == 0 ? 0.f : ldexpf(1.f, l - 5); }
-
 // FP32 difference t = y - x decides x < y outside the guard band [-E, E].
 #define GUARD(t, E, exact) ((t) > (E) ? true : ((t) < -(E) ? false : (exact)))
 
@@ -526,7 +523,8 @@ __global__ void k_dh_tables(int Dy, int W, const double *__restrict__ H, const i
 // over its segments (-inf for an empty column), stored as FP16 rounded up in
 // the column record col[c] = (beg, end, x- | x+ << 16, y- | y+ << 16).
 __global__ void k_dominance(int nx, int ny, const int32_t *__restrict__ beg, const int32_t *__restrict__ end,
-                            const float2 *__restrict__ zf, int4 *__restrict__ col, unsigned *__restrict__ dmask) {
+                            const float2 *__restrict__ zf, int4 *__restrict__ col, unsigned *__restrict__ dmask,
+                            const DomLevels L) {
   const int ncols = nx * ny;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncols) return;
@@ -563,7 +561,7 @@ __global__ void k_dominance(int nx, int ny, const int32_t *__restrict__ beg, con
       cmax[k] = best > cmax[k] ? best : cmax[k];
       if (masked)
         for (int l = 0; l < kDomLevels; ++l)
-          if (best <= dom_level(l)) bits[k][l] |= 1u << (i - k0);
+          if (best <= L.t[l]) bits[k][l] |= 1u << (i - k0);
     }
   }
   if (dmask)
@@ -574,23 +572,26 @@ __global__ void k_dominance(int nx, int ny, const int32_t *__restrict__ beg, con
   col[c] = make_int4(k0, k1, (int)(h[0] | (h[1] << 16)), (int)(h[2] | (h[3] << 16)));
 }
 
+static_assert(kDomLevels <= 15, "pair records hold a level in 4 bits, 15 meaning none");
+
 // Largest dominance level whose threshold is <= dh (15: none).
-__device__ __forceinline__ int dom_level_of(float dh) {
+__device__ __forceinline__ int dom_level_of(float dh, const DomLevels &L) {
   int lv = 15;
   for (int l = 0; l < kDomLevels; ++l)
-    if (dom_level(l) <= dh) lv = l;
+    if (L.t[l] <= dh) lv = l;
   return lv;
 }
 
 // Pair records: (a | d << 8 | x-step level << 16 | y-step level << 20 as
 // float bits, H in FP32, dH x step, dH y step).
 __global__ void k_pair_records(const int2 *__restrict__ pairs, int npairs, const float *__restrict__ Hf,
-                               const float *__restrict__ dH, int W, int dHy, float4 *__restrict__ prec) {
+                               const float *__restrict__ dH, int W, int dHy, float4 *__restrict__ prec,
+                               const DomLevels L) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= npairs) return;
   const int a = pairs[p].x, d = pairs[p].y;
   const float dx = dH[d * W + a], dy = dH[dHy + d * W + a];
-  const int code = a | (d << 8) | (dom_level_of(dx) << 16) | (dom_level_of(dy) << 20);
+  const int code = a | (d << 8) | (dom_level_of(dx, L) << 16) | (dom_level_of(dy, L) << 20);
   prec[p] = make_float4(__int_as_float(code), Hf[d * W + a], dx, dy);
 }
 
@@ -815,7 +816,8 @@ int dilate_fast(vo_ctx *ctx, double R, const vo_volume *in, vo_volume **out, vo_
     cudaMemcpyAsync(dpairs, pairs.data(), sizeof(int2) * pairs.size(), cudaMemcpyHostToDevice, ctx->stream);
     cudaMemsetAsync(ctx->d_flags, 0, 3 * sizeof(int), ctx->stream);  // [0] tier-2 list, [1] fatal, [2] FP64 list
     cudaEventRecord(ctx->ev[0], ctx->stream);
-    fast_prepare(ctx->stream, nx, ny, in->offs, in->offs + 1, in->z, zf, dmax, (float)R, dE, col, dmask);
+    fast_prepare(ctx->stream, nx, ny, in->offs, in->offs + 1, in->z, zf, dmax, (float)R, dE, col, dmask,
+                 T->host.dom);
     fast_pair_records(ctx->stream, dpairs, (int)pairs.size(), *T, prec);
     ctx->launches += 4;
     cudaEventRecord(ctx->ev[1], ctx->stream);
@@ -922,18 +924,20 @@ std::vector<int2> fast_pairs(const Tables &h) {
 }
 
 void fast_prepare(cudaStream_t st, int nx, int ny, const int32_t *beg, const int32_t *end, const double2 *z,
-                  float *zf, unsigned int *maxbits, float R, float *E, int4 *col, unsigned *dmask) {
+                  float *zf, unsigned int *maxbits, float R, float *E, int4 *col, unsigned *dmask,
+                  const DomLevels &L) {
   const int ncols = nx * ny;
   cudaMemsetAsync(maxbits, 0, sizeof(unsigned int), st);
   k_to_f32_cols<<<(ncols + 255) / 256, 256, 0, st>>>(ncols, beg, end, (const double *)z, zf, maxbits);
   k_guard<<<1, 1, 0, st>>>(maxbits, R, E);
   k_dominance<<<(ncols + 127) / 128, 128, 0, st>>>(nx, ny, beg, end, reinterpret_cast<const float2 *>(zf), col,
-                                                    dmask);
+                                                    dmask, L);
 }
 
 void fast_pair_records(cudaStream_t st, const int2 *pairs, int npairs, const DeviceTables &T, float4 *prec) {
   const int W = T.host.W;
-  k_pair_records<<<(npairs + 127) / 128, 128, 0, st>>>(pairs, npairs, T.Hf, T.dH, W, (T.host.Dy + 1) * W, prec);
+  k_pair_records<<<(npairs + 127) / 128, 128, 0, st>>>(pairs, npairs, T.Hf, T.dH, W, (T.host.Dy + 1) * W, prec,
+                                                       T.host.dom);
 }
 
 void launch_dh_tables(cudaStream_t st, int Dy, int W, const double *H, const int *Dx, float *dH) {

@@ -17,6 +17,16 @@ namespace vo {
 constexpr int kCapSmall = 32;    // pass-1 touching-merged piece list / pass-2 union
 constexpr int kCapLarge = 2048;  // overflow re-run capacity per column
 
+// Dominance levels of the FP32 kernels: a segment is dominated at level l
+// in a direction when its width there is <= t[l]; a pair uses the largest
+// level whose threshold is <= its FP32 lower bound of the growth of H. Any
+// thresholds keep the pruning exact; t[0] = 0 and the others are quantiles of
+// the pairs' growths for the radius, so that levels fall where pairs are.
+constexpr int kDomLevels = 15;  // 15 in a pair record means "no level"
+struct DomLevels {
+  float t[kDomLevels];
+};
+
 // Radius tables, computed on the host with the reference's own FP64
 // expressions (so device results match bit for bit) and uploaded once per
 // (radius, grid extent).
@@ -29,6 +39,7 @@ struct Tables {
   std::vector<double> H;      // [(Dy+1)*W] sqrt(r1*r1 - dx*dx), NaN beyond Dx
   std::vector<float> Hf;      // FP32 rounding of H
   std::vector<double> HB;     // [(Dy+1)^2] brute force sqrt(R*R - dx^2 - dy^2), NaN outside
+  DomLevels dom{};            // dominance level thresholds for this radius
 };
 
 // Device view of the tables (kernel argument by value).
@@ -182,7 +193,6 @@ struct FastArgs {
   // neighbour segment widened by the level's threshold.
   const unsigned *dmask;
 };
-constexpr int kDomLevels = 8;
 
 // One dilation of a batch (device array element of the persistent kernel).
 constexpr int kSizerTile = 32;  // side of a sizing tile (columns)
@@ -212,7 +222,8 @@ std::vector<int2> fast_pairs(const Tables &h);
 // FP32 copies of the values of a slot volume, the guard band scalar, the
 // column records (ncols int4) and the dominance masks (4 * kDomLevels * ncols).
 void fast_prepare(cudaStream_t st, int nx, int ny, const int32_t *beg, const int32_t *end, const double2 *z,
-                  float *zf, unsigned int *maxbits, float R, float *E, int4 *col, unsigned *dmask);
+                  float *zf, unsigned int *maxbits, float R, float *E, int4 *col, unsigned *dmask,
+                  const DomLevels &L);
 // Pair records (npairs float4) from the device tables of radius T.
 void fast_pair_records(cudaStream_t st, const int2 *pairs, int npairs, const DeviceTables &T, float4 *prec);
 // Union capacity (24, 32 or 64) of the main FP32 kernels for inputs with the
