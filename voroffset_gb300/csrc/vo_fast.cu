@@ -118,20 +118,21 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
   int n = 0;
   bool overflow = false;
 #define SV(k) sv[(k) * stride]
-  // The records of pair p + 1 (its table entry, its four source columns'
-  // records and their segment dominance masks at the pair's levels) are
-  // loaded while pair p's candidates are merged.
+  // Per pair: its four source columns' records and their segment dominance
+  // masks at the pair's levels, loaded when the pair starts (only the pair's
+  // own table entry is loaded one pair ahead: holding the source records
+  // across the merge loop cost more in register spills than their load
+  // latency, which the other resident warps hide).
   // Source S: x + a if S & 1 (its neighbour toward the output is at x - 1,
   // direction "x-" = 0), else x - a ("x+" = 1); likewise y with S & 2
   // ("y-" = 2, "y+" = 3).
   const int ncols = A.nx * A.ny;
 #define MASK(DIR, LV, C) ((LV) < kDomLevels ? A.dmask[((DIR) * kDomLevels + (LV)) * ncols + (C)] : 0u)
-#define LOAD_ONE(OK, XS, YS, S, R, MX, MY)                                                              \
+#define LOAD_ONE(OK, XS, YS, S, R, D)                                                                   \
   {                                                                                                     \
     const int c_ = (OK) ? (XS) + A.nx * (YS) : 0;                                                       \
     R = (OK) ? A.col[c_] : make_int4(0, 0, 0, 0);                                                       \
-    MX = (OK) ? MASK((S) & 1 ? 0 : 1, lx_, c_) : 0u;                                                    \
-    MY = (OK) ? MASK((S) & 2 ? 2 : 3, ly_, c_) : 0u;                                                    \
+    D = (OK) ? (MASK((S) & 1 ? 0 : 1, lx_, c_) | MASK((S) & 2 ? 2 : 3, ly_, c_)) : 0u;                  \
   }
 #define LOAD_SOURCES(PR)                                                                                \
   {                                                                                                     \
@@ -139,23 +140,18 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
     const int lx_ = (ad_ >> 16) & 0xf, ly_ = (ad_ >> 20) & 0xf;                                         \
     const bool xm = x - a_ >= 0, xp = a_ > 0 && x + a_ < A.nx;                                          \
     const bool ym = y - d_ >= 0, yp = d_ > 0 && y + d_ < A.ny;                                          \
-    LOAD_ONE(xm && ym, x - a_, y - d_, 0, r0, mx0, my0)                                                 \
-    LOAD_ONE(xp && ym, x + a_, y - d_, 1, r1, mx1, my1)                                                 \
-    LOAD_ONE(xm && yp, x - a_, y + d_, 2, r2, mx2, my2)                                                 \
-    LOAD_ONE(xp && yp, x + a_, y + d_, 3, r3, mx3, my3)                                                 \
+    LOAD_ONE(xm && ym, x - a_, y - d_, 0, c0, d0)                                                       \
+    LOAD_ONE(xp && ym, x + a_, y - d_, 1, c1, d1)                                                       \
+    LOAD_ONE(xm && yp, x - a_, y + d_, 2, c2, d2)                                                       \
+    LOAD_ONE(xp && yp, x + a_, y + d_, 3, c3, d3)                                                       \
   }
   float4 pr = A.prec[0];
-  int4 r0, r1, r2, r3;
-  unsigned mx0, my0, mx1, my1, mx2, my2, mx3, my3;
-  LOAD_SOURCES(pr)
   for (int p = 0; p < A.npairs; ++p) {
     const float4 pc = pr;
-    const int4 c0 = r0, c1 = r1, c2 = r2, c3 = r3;
-    const unsigned d0 = mx0 | my0, d1 = mx1 | my1, d2 = mx2 | my2, d3 = mx3 | my3;
-    if (p + 1 < A.npairs) {
-      pr = A.prec[p + 1];
-      LOAD_SOURCES(pr)
-    }
+    if (p + 1 < A.npairs) pr = A.prec[p + 1];
+    int4 c0, c1, c2, c3;
+    unsigned d0, d1, d2, d3;
+    LOAD_SOURCES(pc)
     const int ad = __float_as_int(pc.x), a = ad & 0xff, d = (ad >> 8) & 0xff;
     const float h = pc.y;
     const int da = d | (a << 8);
