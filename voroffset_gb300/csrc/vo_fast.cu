@@ -131,7 +131,7 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
 #define LOAD_ONE(OK, XS, YS, S, R, D)                                                                   \
   {                                                                                                     \
     const int c_ = (OK) ? (XS) + A.nx * (YS) : 0;                                                       \
-    R = (OK) ? A.col[c_] : make_int4(0, 0, 0, 0);                                                       \
+    R = (OK) ? reinterpret_cast<const int2 *>(A.col)[2 * c_] : make_int2(0, 0);                          \
     D = (OK) ? (MASK((S) & 1 ? 0 : 1, lx_, c_) | MASK((S) & 2 ? 2 : 3, ly_, c_)) : 0u;                  \
   }
 #define LOAD_SOURCES(PR)                                                                                \
@@ -149,7 +149,7 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
   for (int p = 0; p < A.npairs; ++p) {
     const float4 pc = pr;
     if (p + 1 < A.npairs) pr = A.prec[p + 1];
-    int4 c0, c1, c2, c3;
+    int2 c0, c1, c2, c3;  // (beg, end) of each source column
     unsigned d0, d1, d2, d3;
     LOAD_SOURCES(pc)
     const int ad = __float_as_int(pc.x), a = ad & 0xff, d = (ad >> 8) & 0xff;
@@ -163,20 +163,27 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
     const __half dhx_h = __float2half_rd(dhx), dhy_h = __float2half_rd(dhy);
     // Per source: [kb, ke) and the mask of its kept segments (bit j: segment
     // kb + j); a source of more than 32 segments keeps all (m = 0, dense).
-#define SRC(S, C, DM, KB, KE, M)                                                                        \
+    // A source of up to 32 segments that is dominated whole has an empty kept
+    // mask; a source of more segments (no masks) is tested with its column
+    // widths.
+#define SRC(S, XS, YS, C, DM, KB, KE, M)                                                                \
   {                                                                                                     \
-    const bool dom = __hle(half_of((unsigned)(C).z, (S) & 1), dhx_h) || __hle(half_of((unsigned)(C).w, (S) & 2), dhy_h); \
-    KB = dom ? 0 : (C).x;                                                                               \
-    KE = dom ? 0 : (C).y;                                                                               \
+    KB = (C).x;                                                                                         \
+    KE = (C).y;                                                                                         \
     const int ns_ = KE - KB;                                                                            \
+    if (ns_ > 32) {                                                                                     \
+      const int4 cr_ = A.col[(XS) + A.nx * (YS)];                                                       \
+      if (__hle(half_of((unsigned)cr_.z, (S) & 1), dhx_h) || __hle(half_of((unsigned)cr_.w, (S) & 2), dhy_h)) \
+        KE = KB;                                                                                        \
+    }                                                                                                   \
     M = ns_ <= 32 ? ~(DM) & (ns_ == 32 ? 0xffffffffu : ((1u << ns_) - 1u)) : 0u;                        \
   }
     int kb0, ke0, kb1, ke1, kb2, ke2, kb3, ke3;
     unsigned m0, m1, m2, m3;
-    SRC(0, c0, d0, kb0, ke0, m0)
-    SRC(1, c1, d1, kb1, ke1, m1)
-    SRC(2, c2, d2, kb2, ke2, m2)
-    SRC(3, c3, d3, kb3, ke3, m3)
+    SRC(0, x - a, y - d, c0, d0, kb0, ke0, m0)
+    SRC(1, x + a, y - d, c1, d1, kb1, ke1, m1)
+    SRC(2, x - a, y + d, c2, d2, kb2, ke2, m2)
+    SRC(3, x + a, y + d, c3, d3, kb3, ke3, m3)
 #undef SRC
 #define KEPT(KB, KE, M) ((KE) - (KB) > 32 ? (KE) - (KB) : __popc(M))
     const int total = KEPT(kb0, ke0, m0) + KEPT(kb1, ke1, m1) + KEPT(kb2, ke2, m2) + KEPT(kb3, ke3, m3);
