@@ -269,7 +269,8 @@ std::vector<int2> build_queue(const std::vector<DilPlan> &dils, int fby) {
   std::vector<int2> q;
   for (const auto &o : order) {
     const vo_grid &g = dils[o.second].in.grid;
-    const int tiles = ((g.nx + kFastCols - 1) / kFastCols) * ((g.ny + fby - 1) / fby);
+    const int bw = kPatchX * fby;  // a block's columns: bw x kPatchY
+    const int tiles = ((g.nx + bw - 1) / bw) * ((g.ny + kPatchY - 1) / kPatchY);
     for (int t = 0; t < tiles; ++t) q.push_back(make_int2(o.second, t));
   }
   return q;

@@ -46,9 +46,9 @@ namespace {
 
 constexpr int kKA = kUnionCap;     // union capacity of the main kernels
 constexpr int kKM = kUnionCapMid;  // union capacity of the second tier
-// Block shape of k_fast: one row of 32 columns (a warp), at most 64 registers
-// so that 32 warps fit an SM; measured faster than 32 x 4 blocks at 80
-// registers (305 vs 340 ms on the 2048^2 r=32 dilation).
+// Block shape of k_fast: one warp (one patch of columns), at most 64
+// registers so that 32 warps fit an SM; measured faster than four-warp blocks
+// at 80 registers (305 vs 340 ms on the 2048^2 r=32 dilation).
 constexpr int kFB = kFastCols, kFBY = 1;
 constexpr int kBigCap = 8192;    // FP64 fallback working list (intervals)
 constexpr int kBigThreads = 32;
@@ -340,8 +340,8 @@ __global__ void __launch_bounds__(kFB *kFBY, 1024 / (kFB * kFBY)) k_fast(FastArg
                                                     int *ovf_count, int *ovf_cols) {
   extern __shared__ float2 sv_dyn[];
   const int tid = threadIdx.x + kFB * threadIdx.y;
-  const int x = blockIdx.x * kFB + threadIdx.x;
-  const int y = blockIdx.y * kFBY + threadIdx.y;
+  const int x = blockIdx.x * kPatchX + threadIdx.x % kPatchX;
+  const int y = blockIdx.y * kPatchY + threadIdx.x / kPatchX;
   if (x >= A.nx || y >= A.ny) return;
   const int c = x + A.nx * y;
   const float E = *A.E;
@@ -658,9 +658,10 @@ __global__ void __launch_bounds__(kFB *FBY, LBN / (kFB * FBY)) k_fast_batched(co
     __syncthreads();
     const BatchVol &V = s_vol;
     const int nx = V.A.nx, ny = V.A.ny;
-    const int tiles_x = (nx + kFB - 1) / kFB;
-    const int x = (q.y % tiles_x) * kFB + threadIdx.x;
-    const int y = (q.y / tiles_x) * FBY + threadIdx.y;
+    const int bw = kPatchX * FBY;  // the item's columns: bw x kPatchY, warp w at x offset w * kPatchX
+    const int tiles_x = (nx + bw - 1) / bw;
+    const int x = (q.y % tiles_x) * bw + threadIdx.y * kPatchX + threadIdx.x % kPatchX;
+    const int y = (q.y / tiles_x) * kPatchY + threadIdx.x / kPatchX;
     if (x < nx && y < ny) {
       const int c = x + nx * y;
       UnionIds<KA> U;
@@ -827,7 +828,7 @@ int dilate_fast(vo_ctx *ctx, double R, const vo_volume *in, vo_volume **out, vo_
   }
   FastArgs A{nx, ny, h.W, in->offs, in->offs + 1, (const double *)in->z, zf, T->Hf, T->H, dpairs,
              (int)pairs.size(), dE, col, prec, dmask};
-  const dim3 blk(kFB, kFBY), grd((nx + kFB - 1) / kFB, (ny + kFBY - 1) / kFBY);
+  const dim3 blk(kFB, kFBY), grd((nx + kPatchX - 1) / kPatchX, (ny + kPatchY - 1) / kPatchY);
   // union capacity from the input's mean segment count per column (24, 32,
   // 48 or 64; dense inputs take 48 up to 24 segments per column, which keeps
   // more warps per SM than 64, the rest going to the second tier)
