@@ -400,10 +400,12 @@ def main():
     vin = ctx.upload(grid, offs, z)
     ctx.sync()
 
-    def timed(step, steps, warmup):
+    def timed(step, steps, warmup, after_warmup=None):
         """Device time (CUDA events on the library stream) of `steps` calls of step()."""
         for _ in range(warmup):
             step()
+        if after_warmup is not None:
+            after_warmup()
         barrier()
         ev0 = torch.cuda.Event(enable_timing=True)
         ev1 = torch.cuda.Event(enable_timing=True)
@@ -445,13 +447,11 @@ def main():
     # ---------------- device-resident arm (value)
     clocks = ClockSampler(local)
     clocks.start()
-    dev_ms = timed(step, args.steps, args.warmup)
+    # launches and kernel time are counted over the timed steps only
+    dev_ms = timed(step, args.steps, args.warmup, after_warmup=lambda: acc.update(launches=0, kernel_ms=0.0))
     clk = clocks.stop()
-    launches, kernel_total_ms, out_segs, mid = acc["launches"], acc["kernel_ms"], acc["out_segs"], acc["mid"]
+    launches, kernel_ms, out_segs, mid = acc["launches"], acc["kernel_ms"], acc["out_segs"], acc["mid"]
     value = job_rate(world, ncols * args.steps, dev_ms / 1e3)
-    # kernel time of the warm-up steps was accumulated too: keep the timed steps only
-    kernel_ms = kernel_total_ms * args.steps / (args.steps + args.warmup)
-    launches = launches * args.steps // (args.steps + args.warmup)
 
     # ---------------- comparison arms on the same volume: the plain GPU method
     # (FP64 separable, count then fill) and the single-volume FP32-guarded method

@@ -103,13 +103,13 @@ def test_pruned_union_equals_oracle(vo, oracle, R, seed):
     assert kept < total  # the rule prunes something on these shapes
 
 
-NLEVELS = 15
+NLEVELS = 11
 
 
 def _levels(H):
     """Dominance level thresholds of a radius, as the library's table builder
     sets them: 0, then the growths of H over one lattice step (FP32 lower
-    bounds) at quantiles (l - 1/2) / 14 of their sorted list."""
+    bounds) at quantiles (l - 1/2) / (NLEVELS - 1) of their sorted list."""
     g = sorted([_down(H[(d, a - 1)] - H[(d, a)]) for (d, a) in H if a >= 1] +
                [_down(H[(d - 1, a)] - H[(d, a)]) for (d, a) in H if d >= 1])
     t = [0.0]

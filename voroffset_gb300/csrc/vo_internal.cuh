@@ -22,7 +22,7 @@ constexpr int kCapLarge = 2048;  // overflow re-run capacity per column
 // level whose threshold is <= its FP32 lower bound of the growth of H. Any
 // thresholds keep the pruning exact; t[0] = 0 and the others are quantiles of
 // the pairs' growths for the radius, so that levels fall where pairs are.
-constexpr int kDomLevels = 15;  // 15 in a pair record means "no level"
+constexpr int kDomLevels = 11;  // 15 in a pair record means "no level"
 struct DomLevels {
   float t[kDomLevels];
 };
