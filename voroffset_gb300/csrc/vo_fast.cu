@@ -186,37 +186,36 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
     SRC(3, x + a, y + d, c3, d3, kb3, ke3, m3)
 #undef SRC
 #define KEPT(KB, KE, M) ((KE) - (KB) > 32 ? (KE) - (KB) : __popc(M))
-    const int total = KEPT(kb0, ke0, m0) + KEPT(kb1, ke1, m1) + KEPT(kb2, ke2, m2) + KEPT(kb3, ke3, m3);
+    const int t0 = KEPT(kb0, ke0, m0), t1 = KEPT(kb1, ke1, m1), t2 = KEPT(kb2, ke2, m2), t3 = KEPT(kb3, ke3, m3);
 #undef KEPT
+    const int total = t0 + t1 + t2 + t3;
     const int iters = __reduce_max_sync(mask, total);
-    // Walk state: source s, its remaining mask ms (sparse) or next index kc
-    // (dense); NEXT yields the next kept candidate (KN, SN), or KN = -1.
+    // Walk state: the sources still to visit that keep candidates (bit s),
+    // the current source s, its remaining mask ms (sparse) or next index kc
+    // (dense); NEXT yields the next kept candidate (KN, SN), or KN = -1. A
+    // source is entered only when it keeps a candidate, so NEXT takes at most
+    // one source switch and no loop.
+    unsigned srcs = (t0 > 0 ? 1u : 0u) | (t1 > 0 ? 2u : 0u) | (t2 > 0 ? 4u : 0u) | (t3 > 0 ? 8u : 0u);
     int s = -1, kc = 0, kend = 0, kbs = 0;
     unsigned ms = 0;
     bool dense = false;
 #define NEXT(KN, SN)                                                                                    \
   {                                                                                                     \
-    KN = -1;                                                                                            \
-    for (;;) {                                                                                          \
-      if (s >= 0) {                                                                                     \
-        if (dense) {                                                                                    \
-          if (kc < kend) {                                                                              \
-            KN = kc++;                                                                                  \
-            break;                                                                                      \
-          }                                                                                             \
-        } else if (ms) {                                                                                \
-          KN = kbs + __ffs(ms) - 1;                                                                     \
-          ms &= ms - 1;                                                                                 \
-          break;                                                                                        \
-        }                                                                                               \
-      }                                                                                                 \
-      if (s >= 3) break;                                                                                \
-      ++s;                                                                                              \
+    if ((dense ? kc >= kend : ms == 0u) && srcs) {                                                      \
+      s = __ffs(srcs) - 1;                                                                              \
+      srcs &= srcs - 1;                                                                                 \
       kbs = s == 0 ? kb0 : s == 1 ? kb1 : s == 2 ? kb2 : kb3;                                           \
       kend = s == 0 ? ke0 : s == 1 ? ke1 : s == 2 ? ke2 : ke3;                                          \
       ms = s == 0 ? m0 : s == 1 ? m1 : s == 2 ? m2 : m3;                                                \
       dense = kend - kbs > 32;                                                                          \
       kc = kbs;                                                                                         \
+    }                                                                                                   \
+    KN = -1;                                                                                            \
+    if (dense) {                                                                                        \
+      if (kc < kend) KN = kc++;                                                                         \
+    } else if (ms) {                                                                                    \
+      KN = kbs + __ffs(ms) - 1;                                                                         \
+      ms &= ms - 1;                                                                                     \
     }                                                                                                   \
     SN = s;                                                                                             \
   }
