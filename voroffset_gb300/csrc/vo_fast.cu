@@ -118,6 +118,11 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
   int n = 0;
   bool overflow = false;
 #define SV(k) sv[(k) * stride]
+  // SV(n) holds a sentinel above every value, so the cursor walk stops at
+  // the end of the union without a bounds test; the union holds up to KA - 1
+  // intervals.
+  const float2 kTop = make_float2(INFINITY, INFINITY);
+  SV(0) = kTop;
   // Per pair: its four source columns' records and their segment dominance
   // masks at the pair's levels, loaded when the pair starts (only the pair's
   // own table entry is loaded one pair ahead: holding the source records
@@ -233,24 +238,24 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
         if (src != cur_src) {  // first candidate of a new source column: restart the cursor
           cur_src = src;
           cur = 0;
-          if (n > 0) cv = SV(0);
+          cv = SV(0);
         }
         {
           const float lo = zf.x - h, hi = zf.y + h;
           const int il = 2 * k, ih = 2 * k + 1;
           // skip union intervals that end strictly below the candidate: U.hi[cur] < lo
           // (the next interval's values are loaded one step ahead)
-          if (cur < n && lo - cv.y > E) {
-            float2 cn = cur + 1 < n ? SV(cur + 1) : cv;
+          if (lo - cv.y > E) {
+            float2 cn = SV(min(cur + 1, n));
             do {
               ++cur;
               cv = cn;
-              if (cur + 1 < n) cn = SV(cur + 1);
-            } while (cur < n && lo - cv.y > E);
+              cn = SV(min(cur + 1, n));
+            } while (lo - cv.y > E);
           }
           while (cur < n && GUARD(lo - cv.y, E, ex_u_lt_c(A, U, cur, true, il, da, false))) {
             ++cur;
-            if (cur < n) cv = SV(cur);
+            cv = SV(cur);
           }
           bool covered = false;
           if (cur < n) {
@@ -264,7 +269,7 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
           if (!covered) {
             if (cur == n || GUARD(cv.x - hi, E, ex_c_lt_u(A, U, ih, da, true, cur, false))) {
               // disjoint: insert before cur
-              if (n >= KA) {
+              if (n >= KA - 1) {
                 overflow = true;
               } else {
                 for (int j = n; j > cur; --j) {
@@ -277,6 +282,7 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
                 U.lo[cur] = make_int2(il, da);
                 U.hi[cur] = make_int2(ih, da);
                 ++n;
+                SV(n) = kTop;
               }
             } else {
               // overlapping or touching U[cur]: extend it
@@ -306,6 +312,7 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
                     U.hi[m] = U.hi[m + gone];
                   }
                   n -= gone;
+                  SV(n) = kTop;
                 }
               }
               SV(cur) = cv;
