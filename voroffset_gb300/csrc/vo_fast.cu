@@ -245,13 +245,23 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
           const int il = 2 * k, ih = 2 * k + 1;
           // skip union intervals that end strictly below the candidate: U.hi[cur] < lo
           // (the next interval's values are loaded one step ahead)
-          if (lo - cv.y > E) {
-            float2 cn = SV(min(cur + 1, n));
-            do {
-              ++cur;
-              cv = cn;
-              cn = SV(min(cur + 1, n));
-            } while (lo - cv.y > E);
+          if (lo - cv.y > E) {  // two intervals per step: cur < n here, so cur + 1 <= n
+            float2 c1 = SV(cur + 1), c2 = SV(min(cur + 2, n));
+            for (;;) {
+              if (!(lo - c1.y > E)) {
+                cur += 1;
+                cv = c1;
+                break;
+              }
+              if (!(lo - c2.y > E)) {
+                cur += 2;
+                cv = c2;
+                break;
+              }
+              cur += 2;
+              c1 = SV(cur + 1);
+              c2 = SV(min(cur + 2, n));
+            }
           }
           while (cur < n && GUARD(lo - cv.y, E, ex_u_lt_c(A, U, cur, true, il, da, false))) {
             ++cur;
