@@ -331,7 +331,10 @@ int tune_shape(vo_ctx *ctx, vo_batch *b, const std::vector<DilPlan> &dils, const
     // four contiguous runs of the queue, evenly spaced: neighbouring tiles run
     // together as in the real launch, so the sample sees its cache reuse
     const std::vector<int2> full = build_queue(dils, fby);
-    const size_t want = std::min(full.size(), std::max<size_t>(512, full.size() / 16));
+    // at least two waves of resident blocks: a sample smaller than a wave
+    // times the tail of a partly idle GPU, not the throughput of a full one
+    const size_t waves = (size_t)2 * sms * per_sm;
+    const size_t want = std::min(full.size(), std::max<size_t>({512, full.size() / 16, waves}));
     std::vector<int2> sample;
     for (int r = 0; r < 4; ++r) {
       const size_t len = want / 4 + (r < (int)(want % 4) ? 1 : 0);
