@@ -134,8 +134,8 @@ typedef struct vo_batch vo_batch;
 typedef struct {
   int64_t slot_bytes;   /* output slot memory of the dilations */
   int32_t tiles;        /* work-queue items over all rounds */
-  int32_t tile_rows;    /* rows of 32 columns per block chosen by the autotuner (last round): 1, 2 or 4 */
-  int32_t union_cap;    /* union intervals per column of the main kernel (last round): 24, 32 or 64 */
+  int32_t tile_rows;    /* warps (8 x 4 column patches) per block chosen by the autotuner (last round): 1, 2 or 4 */
+  int32_t union_cap;    /* union slots per column of the main kernel (last round): 24, 32, 48 or 64; one holds a sentinel */
   int32_t persistent;   /* 1: one wave of blocks pulling queue items; 0: one block per item (last round) */
   int32_t regs;         /* register budget per thread of the batch kernel (last round): 64 or 80 */
   int32_t graph_nodes;  /* nodes of the captured graph */

@@ -18,9 +18,10 @@
 //   * work queue: dilations in decreasing predicted total work (the network's
 //     per-tile candidate counts, or the mean cost per column), the tiles of
 //     each in raster order;
-//   * union capacity of the main kernel (24 or 32; 64 for dense inputs, more
-//     than 10 segments per column on average) and block shape (rows of 32
-//     columns per block), chosen by the autotuner below and cached per context.
+//   * union capacity of the main kernel (24 or 32; 48 or 64 for dense inputs,
+//     more than 10 segments per column on average), block shape (1, 2 or 4
+//     warps of 8 x 4 columns per block), register budget and launch mode,
+//     chosen by the autotuner below and cached per context.
 // Then the closures are captured into one graph. vo_batch_run replays it and
 // re-runs, through the single-volume path, every volume whose overflow flag
 // is set (a union larger than its slot with the spill region exhausted, or

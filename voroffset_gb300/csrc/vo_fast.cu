@@ -105,7 +105,7 @@ __device__ __forceinline__ float half_lo_hi(unsigned v, int lo) {
 #define GUARD(t, E, exact) ((t) > (E) ? true : ((t) < -(E) ? false : (exact)))
 
 // Returns the number of intervals of the union (identities in U), or -1 when
-// more than KA are needed.
+// more than KA - 1 are needed (the last of the KA slots holds the sentinel).
 //
 // `mask` holds the lanes of the warp running this function together. For each
 // (|dx|, |dy|) pair the four source columns' segments form one list per lane;
@@ -348,7 +348,7 @@ __device__ __forceinline__ void write_union(const FastArgs &A, const UnionIds<KA
 }
 
 // One pass: the exact union of every output column goes to its fixed-capacity
-// staging slot (KA intervals) with its count; columns that need more are
+// staging slot (KA entries, at most KA - 1 used) with its count; columns that need more are
 // listed for the second tier. A compaction pass then packs the slots.
 template <int KA>
 __global__ void __launch_bounds__(kFB *kFBY, 1024 / (kFB * kFBY)) k_fast(FastArgs A, int32_t *counts,
@@ -387,8 +387,8 @@ __global__ void k_compact(int ncols, int ka, const int32_t *__restrict__ counts,
 }
 
 // Second tier over the columns listed by k_fast (grid-stride): the same
-// computation with kKM intervals. Count pass: counts[c], or the column goes to
-// the FP64 list when even kKM is exceeded. Fill pass: writes the union at its
+// computation with kKM slots (kKM - 1 intervals). Count pass: counts[c], or the
+// column goes to the FP64 list when even that is exceeded. Fill pass: writes the union at its
 // CSR offset (columns of the FP64 list are left to it).
 template <bool FILL>
 __global__ void __launch_bounds__(kMidThreads) k_fast_mid(FastArgs A, int32_t *counts, const int32_t *ooffs,
@@ -641,11 +641,11 @@ __device__ __forceinline__ int place_union(const BatchVol &V, int x, int y, int 
   return dst;
 }
 
-// Persistent kernel over the tiles (kFB x FBY output columns) of every
+// Persistent kernel over the tiles (FBY patches of 8 x 4 output columns) of every
 // dilation of a batch: blocks pull (dilation, tile) items from a queue ordered
 // by decreasing estimated work, so uneven volumes balance across the SMs.
 // Each column's union goes to its slot (place_union); a union of more than
-// KA intervals is listed for k_fast_batched_mid.
+// KA - 1 intervals is listed for k_fast_batched_mid.
 // SINGLE: the round has one dilation, whose arguments come as the kernel
 // parameter A1 (constant bank) instead of from memory.
 // LBN / (kFB * FBY) blocks per SM bound the registers: LBN = 1024 gives 64
@@ -704,8 +704,8 @@ __global__ void __launch_bounds__(kFB *FBY, LBN / (kFB * FBY)) k_fast_batched(co
 }
 
 // Second tier of a batch round: the listed columns of every dilation with
-// kKM intervals, placed like the first tier; a union beyond kKM sets the
-// dilation's overflow flag.
+// kKM slots, placed like the first tier; a union of more than kKM - 1
+// intervals sets the dilation's overflow flag.
 __global__ void __launch_bounds__(kMidThreads) k_fast_batched_mid(const BatchVol *vols, int nv) {
   __shared__ float2 sv[kKM * kMidThreads];
   const int nth = gridDim.x * kMidThreads;
