@@ -267,13 +267,16 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
             ++cur;
             cv = SV(cur);
           }
-          bool covered = false;
+          // covered: inside U[cur]; else ext_lo / ext_hi: the candidate reaches
+          // below / above U[cur] (both decided once, used again to extend it)
+          bool covered = false, ext_lo = false, ext_hi = false;
           if (cur < n) {
             if (lo - cv.x > E && cv.y - hi > E) {
               covered = true;  // inside U[cur] by more than the guard band
             } else {
-              const bool lo_in = !GUARD(cv.x - lo, E, ex_c_lt_u(A, U, il, da, false, cur, false));
-              covered = lo_in && !GUARD(hi - cv.y, E, ex_u_lt_c(A, U, cur, true, ih, da, true));
+              ext_lo = GUARD(cv.x - lo, E, ex_c_lt_u(A, U, il, da, false, cur, false));
+              ext_hi = GUARD(hi - cv.y, E, ex_u_lt_c(A, U, cur, true, ih, da, true));
+              covered = !ext_lo && !ext_hi;
             }
           }
           if (!covered) {
@@ -296,11 +299,11 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
               }
             } else {
               // overlapping or touching U[cur]: extend it
-              if (GUARD(cv.x - lo, E, ex_c_lt_u(A, U, il, da, false, cur, false))) {
+              if (ext_lo) {
                 cv.x = lo;
                 U.lo[cur] = make_int2(il, da);
               }
-              if (GUARD(hi - cv.y, E, ex_u_lt_c(A, U, cur, true, ih, da, true))) {
+              if (ext_hi) {
                 cv.y = hi;
                 U.hi[cur] = make_int2(ih, da);
                 // absorb following intervals that now start at or below the new end
