@@ -96,11 +96,6 @@ __device__ __forceinline__ __half half_of(unsigned v, int lo) {
   return __ushort_as_half((unsigned short)(lo ? (v & 0xffffu) : (v >> 16)));
 }
 
-// The FP16 in the low (lo != 0) or high half of v, as a float.
-__device__ __forceinline__ float half_lo_hi(unsigned v, int lo) {
-  return __half2float(__ushort_as_half((unsigned short)(lo ? (v & 0xffffu) : (v >> 16))));
-}
-
 // FP32 difference t = y - x decides x < y outside the guard band [-E, E].
 #define GUARD(t, E, exact) ((t) > (E) ? true : ((t) < -(E) ? false : (exact)))
 
