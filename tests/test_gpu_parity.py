@@ -134,12 +134,13 @@ def test_gpu_zero_length_and_touching_segments(ctx, vo, oracle, method):
 
 
 @pytest.mark.parametrize("method", METHODS)
-@pytest.mark.parametrize("k", [40, 100, 150])
+@pytest.mark.parametrize("k", [40, 63, 64, 100, 127, 128, 150])
 def test_gpu_overflow_path(ctx, vo, oracle, method, k):
-    # many thin disjoint plates per column overflow the kernels' working lists
-    # (FP32 method: 40 fits its 64-interval variant for dense inputs, 100 needs
-    # the 128-interval second tier, 150 its FP64 list); the large-capacity
-    # re-runs must give the same answer
+    # k thin disjoint plates per column dilated by r = 0.9 give exactly k
+    # union intervals, overflowing the kernels' working lists at known sizes
+    # (FP32 method: its 64-slot variant for dense inputs holds 63 intervals
+    # beside its sentinel, the 128-slot second tier 127, beyond that the
+    # FP64 list); every tier must give the same answer
     nx, ny = 40, 40
     base = np.arange(k, dtype=np.float64) * 3.0
     z = np.stack([base, base + 1.0], 1).reshape(-1)
@@ -148,7 +149,9 @@ def test_gpu_overflow_path(ctx, vo, oracle, method, k):
     grid = vo.Grid(nx, ny, (0, 0, 0), (nx, ny, 3 * k), 1.0, 0)
     want = oracle.morph(ogrid(oracle, grid), offs, zz, 0.9, "dilation")
     got, t = run(ctx, grid, offs, zz, "dilation", 0.9, method)
-    if method != "fast" or k > 64:
+    if method == "fast":
+        assert (t["overflow_columns"] > 0) == (k > 63), t["overflow_columns"]
+    else:
         assert t["overflow_columns"] > 0
     assert_same(got, want, tol=0.0)
 
