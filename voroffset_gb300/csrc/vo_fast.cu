@@ -155,9 +155,8 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
     const int ad = __float_as_int(pc.x), a = ad & 0xff, d = (ad >> 8) & 0xff;
     const float h = pc.y;
     const int da = d | (a << 8);
-    // growth of H over one step toward the output column (x step, y step): a
-    // source column dominated in either direction is skipped whole; of the
-    // others (up to 32 segments), the segments dominated at the pair's levels
+    // growth of H over one step toward the output column (x step, y step),
+    // against which the sources' dominance widths are tested
     const float dhx = pc.z, dhy = pc.w;
     // FP16 bounds of the pair's growths (rounded down) for the source tests
     const __half dhx_h = __float2half_rd(dhx), dhy_h = __float2half_rd(dhy);
