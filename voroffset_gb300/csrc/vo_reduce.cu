@@ -115,12 +115,13 @@ extern "C" int vo_xor_volume(vo_ctx *ctx, const vo_volume *a, const vo_volume *b
 // vo_xor_volume_noalloc runs the same two kernels as vo_xor_volume, but its
 // scratch (one partial sum per block of kThreads columns, plus the result)
 // is the fixed-size array below instead of memory allocated per call. It is
-// for callers that must not allocate device memory while they run: code that
-// executes inside a host callback enqueued on a stream (where CUDA calls that
-// allocate are not permitted), services whose device memory budget is owned
-// by another allocator, and hot loops that must stay off the allocator's
-// locks. Every GPU that loads this library holds the array until the process
-// exits: (kNoAllocMaxBlocks + 1) doubles, 512 KiB + 8 B.
+// for callers that must not allocate device memory while they run: services
+// whose device memory budget is owned by another allocator (a caching pool
+// that must see every byte), and hot loops that must stay off the
+// allocator's locks and its synchronisation. It is called from ordinary host
+// code; like every CUDA call it must not be made from inside a host function
+// enqueued on a stream. Every GPU that loads this library holds the array
+// until the process exits: (kNoAllocMaxBlocks + 1) doubles, 512 KiB + 8 B.
 
 namespace vo {
 namespace {
@@ -131,16 +132,14 @@ constexpr int kNoAllocMaxDevices = 64;
 static __device__ __align__(256) double g_xor_scratch[kNoAllocMaxBlocks + 1];
 
 // Device address of g_xor_scratch, looked up once per device (in host code the
-// symbol itself is only a host-side stand-in and must not be passed to a kernel).
+// symbol itself is only a host-side stand-in and must not be passed to a
+// kernel). The address stays valid for the life of the device's primary
+// context, so a process that uses this entry point must not reset the device
+// (cudaDeviceReset) afterwards.
 double *g_xor_scratch_ptr[kNoAllocMaxDevices] = {};
 std::mutex g_xor_scratch_mutex;
 
-int xor_scratch_for_current_device(double **out) {
-  int dev = -1;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) {
-    cudaGetLastError();
-    return VO_ENODEV;
-  }
+int xor_scratch_for_device(int dev, double **out) {
   std::lock_guard<std::mutex> lock(g_xor_scratch_mutex);
   if (!g_xor_scratch_ptr[dev]) {
     void *p = nullptr;
@@ -163,24 +162,45 @@ extern "C" int vo_xor_volume_noalloc(const vo_grid *grid, const int32_t *offs_a,
   if (!grid || grid->nx <= 0 || grid->ny <= 0 || !volume) return VO_EINVAL;
   const int64_t ncols = (int64_t)grid->nx * grid->ny;
   if (ncols > (int64_t)kNoAllocMaxBlocks * kThreads) return VO_ERANGE;  // beyond the fixed scratch
-  if (!offs_a || !offs_b) return VO_EINVAL;
-  double *scratch = nullptr;
-  int rc = xor_scratch_for_current_device(&scratch);
-  if (rc) return rc;
+  if (!offs_a || !offs_b || !z_a || !z_b) return VO_EINVAL;
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) {
+    cudaGetLastError();
+    return VO_ENODEV;
+  }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (st) {  // the scratch address below is the current device's: the stream must run there
+    int sdev = -1;
+    if (cudaStreamGetDevice(st, &sdev) != cudaSuccess) {
+      cudaGetLastError();
+      return VO_EINVAL;
+    }
+    if (sdev != dev) return VO_EINVAL;
+  }
+  double *scratch = nullptr;
+  int rc = xor_scratch_for_device(dev, &scratch);
+  if (rc) return rc;
   const int nblk = (int)((ncols + kThreads - 1) / kThreads);
   // Every partial sum the reduction reads is written by this call's first
-  // kernel, and the result slot by the second: nothing carries over from the
-  // previous call, so no clearing is needed.
+  // kernel, and the result slot by the second. The result slot is first set
+  // to a NaN pattern (all bytes 0xff), so a reduction that did not run can
+  // never hand back the previous call's volume.
+  if (cudaMemsetAsync(scratch + kNoAllocMaxBlocks, 0xff, sizeof(double), st) != cudaSuccess) {
+    cudaGetLastError();
+    return VO_ECUDA;
+  }
   k_xor<<<nblk, kThreads, 0, st>>>((int)ncols, offs_a, reinterpret_cast<const double2 *>(z_a), offs_b,
                                    reinterpret_cast<const double2 *>(z_b), scratch);
+  if (cudaGetLastError() != cudaSuccess) return VO_ECUDA;
   k_sum<<<1, kThreads, 0, st>>>(scratch, nblk, scratch + kNoAllocMaxBlocks);
+  if (cudaGetLastError() != cudaSuccess) return VO_ECUDA;
   double h = 0;
   if (cudaMemcpyAsync(&h, scratch + kNoAllocMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess) {
     cudaGetLastError();
     return VO_ECUDA;
   }
+  if (h != h) return VO_ECUDA;  // the sentinel survived: the reduction did not complete
   const double sp = grid->spacing;
   *volume = sp * sp * sp * h;
   return VO_OK;
