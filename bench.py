@@ -143,8 +143,13 @@ def traffic_per_column(kernel: str, radius: float):
         return None
 
 
-def cpu_sample(grid, offs, z, radius, target_s, step_rows=None):
-    """Times the CPU reference (or its restatement) on a slab of rows. Returns a dict."""
+def cpu_sample(grid, offs, z, radius, target_s, step_rows=None, gpu_out=None):
+    """Times the CPU reference (or its restatement) on a slab of rows. Returns a dict.
+
+    The slab is a band of `rows` interior rows from the middle of the volume plus a halo of
+    floor(radius) rows on each side; the halo is computed (the interior columns' discs need it) but
+    only the interior columns are counted. With gpu_out = (offs, z) of the GPU's output for the whole
+    volume, the interior columns of the CPU result are also compared with it (`precision`)."""
     from oracle import oracle as O
     kind = "reference" if O.ref_available() else "port"
     cores = os.cpu_count() or 1
@@ -152,40 +157,65 @@ def cpu_sample(grid, offs, z, radius, target_s, step_rows=None):
     nx, ny = grid.nx, grid.ny
 
     def run(rows):
-        y0 = max(0, ny // 2 - rows // 2 - R)
-        y1 = min(ny, y0 + rows + 2 * R)
+        rows = min(rows, ny)
+        yi0 = max(0, ny // 2 - rows // 2)
+        yi1 = min(ny, yi0 + rows)
+        y0, y1 = max(0, yi0 - R), min(ny, yi1 + R)
         sub_offs = offs[y0 * nx:y1 * nx + 1] - offs[y0 * nx]
         sub_z = z[2 * offs[y0 * nx]:2 * offs[y1 * nx]]
         g = O.Grid(nx, y1 - y0, (0.0, 0.0, 0.0), (nx, y1 - y0, grid.extent[2]), 1.0, 0)
-        inner = nx * (y1 - y0)  # every slab column is computed by the same per-column work
         t0 = time.perf_counter()
         if kind == "reference":
-            O.ref_morph(g, sub_offs, sub_z, radius, "dilation", "ours", threads=cores)
+            oo, oz = O.ref_morph(g, sub_offs, sub_z, radius, "dilation", "ours", threads=cores)[:2]
         else:
-            O.dilate_timed(g, sub_offs, sub_z, radius, threads=cores)
-        return time.perf_counter() - t0, inner, y1 - y0
+            oo, oz = O.dilate_timed(g, sub_offs, sub_z, radius, threads=cores)[:2]
+        dt = time.perf_counter() - t0
+        return dt, nx * (yi1 - yi0), (yi0, yi1, y0, y1), (oo, oz)
 
     if step_rows is None:
         rows = 16
-        dt, inner, tot = run(rows)
+        dt, inner, span, res = run(rows)
         while dt < target_s / 4 and rows < ny:
             rows = min(ny, int(rows * max(2.0, 0.5 * target_s / max(dt, 1e-3))))
-            dt, inner, tot = run(rows)
+            dt, inner, span, res = run(rows)
     else:
-        dt, inner, tot = run(step_rows)
         rows = step_rows
+        dt, inner, span, res = run(rows)
+    yi0, yi1, y0, y1 = span
     val = inner / dt / 1e6
-    sample = (f"dilation r={radius:g} of a {nx} x {tot}-row slab cut from the middle of {WORKLOAD}, "
-              f"all {nx * tot} slab columns counted")
-    return {"value": val, "unit": "Mcolumns/s", "cores": cores, "kind": kind, "sample": sample,
-            "seconds": dt, "rows": rows}
+    sample = (f"dilation r={radius:g} of rows {yi0}-{yi1 - 1} ({yi1 - yi0} x {nx} columns counted) from the "
+              f"middle of the volume, computed with a {yi0 - y0}+{y1 - yi1}-row halo that is not counted")
+    out = {"value": val, "unit": "Mcolumns/s", "cores": cores, "kind": kind, "sample": sample,
+           "seconds": dt, "rows": rows}
+    if gpu_out is not None:
+        go, gz = gpu_out
+        c0, c1 = yi0 * nx, yi1 * nx  # interior columns in the whole volume
+        s0 = (yi0 - y0) * nx          # ... and in the slab
+        wo, wz = res
+        a_off = go[c0:c1 + 1] - go[c0]
+        a_z = gz[2 * go[c0]:2 * go[c1]]
+        b_off = wo[s0:s0 + (c1 - c0) + 1] - wo[s0]
+        b_z = wz[2 * wo[s0]:2 * wo[s0 + (c1 - c0)]]
+        cmp = O.compare((a_off, a_z), (b_off, b_z))
+        out["precision"] = {"max_endpoint_error": cmp["max_err"], "topology_mismatches": cmp["count_mismatch"],
+                            "columns_checked": int(c1 - c0),
+                            "checked_against": "the reference build (oracle/_ref)" if kind == "reference"
+                            else "the FP64 oracle restatement"}
+    return out
+
+
+def bench_config(args, grid, offs):
+    """The workload, identical in both arms (method, launch shape and the like go to `run`)."""
+    return {"workload": f"{args.workload} dilation r={args.radius:g}", "grid": [grid.nx, grid.ny],
+            "in_segments": int(offs[-1]), "radius": args.radius}
 
 
 def reference_arm(args, rank, world):
     if rank != 0:
         return 0
-    import voroffset_gb300 as V
-    grid, offs, z = V.workload(args.workload, seed=1)
+    import voroffset_gb300 as V  # parameters only: no product library is loaded by this arm
+    from oracle import oracle as O
+    grid, offs, z = V.workload(args.workload, seed=1, synth=O.SYNTH_SO)
     # calibrate a slab that takes a few seconds per step
     cal = cpu_sample(grid, offs, z, args.radius, target_s=min(args.cpu_seconds, 8.0))
     rows = cal["rows"]
@@ -201,8 +231,7 @@ def reference_arm(args, rank, world):
             "warmup": args.warmup, "ms_per_step": 1e3 * secs / len(vals), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": f"{args.workload} dilation r={args.radius:g}", "grid": [grid.nx, grid.ny],
-                       "in_segments": int(offs[-1]), "parallelism": "host threads"},
+            "config": bench_config(args, grid, offs), "run": {"parallelism": "host threads"},
             "cpu_baseline": {"value": value, "unit": "Mcolumns/s", "cores": vals[0]["cores"],
                              "kind": vals[0]["kind"], "sample": vals[0]["sample"]},
             "e2e": {"value": value, "unit": "Mcolumns/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -509,16 +538,16 @@ def main():
                 "op_achieved": alg_bytes / (dev_ms / args.steps / 1e3) / 1e9}
 
     dtype = "f64" if args.method in ("separable", "brute") else "f32+f64"
-    cfg = {"workload": f"{args.workload} dilation r={args.radius:g}", "grid": [grid.nx, grid.ny],
-           "method": args.method if args.method != "batched" else "batched+learned" if sizer else "batched",
-           "in_segments": int(offs[-1]), "out_segments": int(out_segs), "mid_pieces": int(mid),
+    cfg = bench_config(args, grid, offs)
+    run = {"method": args.method if args.method != "batched" else "batched+learned" if sizer else "batched",
+           "out_segments": int(out_segs), "mid_pieces": int(mid),
            "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas" if world > 1 else "single GPU"}
     if plan_stats is not None:
-        cfg["plan"] = {k: plan_stats[k] for k in ("slot_bytes", "tiles", "tile_rows", "union_cap", "persistent", "regs", "graph_nodes",
+        run["plan"] = {k: plan_stats[k] for k in ("slot_bytes", "tiles", "tile_rows", "union_cap", "persistent", "regs", "graph_nodes",
                                                   "graph_kernels", "learned", "plan_ms", "tune_ms")}
     line = {"metric": METRIC, "value": value, "unit": "Mcolumns/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic", "config": cfg,
+            "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic", "config": cfg, "run": run,
             "e2e": {"value": e2e, "unit": "Mcolumns/s", "h2d_bytes_per_step": int(in_bytes),
                     "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(launches),
@@ -526,8 +555,9 @@ def main():
             "gsegments_per_s": world * (int(offs[-1]) + int(out_segs)) * args.steps / (dev_ms / 1e3) / 1e9}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
-            line["cpu_baseline"] = {k: v for k, v in cpu_sample(grid, offs, z, args.radius,
-                                                               args.cpu_seconds).items() if k != "rows"}
+            cb = cpu_sample(grid, offs, z, args.radius, args.cpu_seconds, gpu_out=(out_offs, out_z[:2 * out_segs]))
+            line["precision"] = cb.pop("precision")
+            line["cpu_baseline"] = {k: v for k, v in cb.items() if k != "rows"}
         except Exception as exc:  # the baseline is reported, never required
             line["cpu_baseline"] = {"value": None, "error": str(exc)}
     if plan is not None:

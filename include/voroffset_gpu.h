@@ -34,7 +34,8 @@ extern "C" {
 #define VO_EINVAL -1    /* bad argument */
 #define VO_ENOMEM -2    /* host or device allocation failed */
 #define VO_ECUDA -3     /* CUDA runtime error (message in vo_last_error) */
-#define VO_ERADIUS -4   /* radius a hair below a lattice distance (see DESIGN) */
+#define VO_ERADIUS -4   /* radius within rounding of a lattice distance: its lattice reach would
+                           depend on the column position (floor(x + r) != x + floor(r)) */
 #define VO_ERANGE -5    /* result does not fit int32 CSR offsets */
 #define VO_ENODEV -6    /* no usable sm_103 device */
 #define VO_ETIMEOUT -7  /* a device-side bounded wait gave up */
@@ -164,22 +165,32 @@ void vo_batch_destroy(vo_ctx *ctx, vo_batch *b);
 int vo_dexelize(vo_ctx *ctx, const double *verts, int nv, const int32_t *tris, int nt,
                 double *spacing, int padding, int num_dexels, vo_volume **out);
 
+/* Columns of this context's last successful vo_dexelize whose ray met the mesh
+ * an odd number of times (an open or self-intersecting mesh). The reference
+ * keeps such a column's odd value list (Dexelize.cpp:208-213), but every
+ * consumer reads values in pairs (CompressedVolume::iterate), so its last hit
+ * is never used; the CSR pairs here have no place for it and drop it. */
+int vo_dexelize_odd_columns(vo_ctx *ctx, int64_t *count);
+
 /* Xor volume of two volumes on the same grid (Voronoi.cpp:91-111,
  * calculateXor's return value), computed on the device. */
 int vo_xor_volume(vo_ctx *ctx, const vo_volume *a, const vo_volume *b, double *volume);
 
 /* Allocation-free xor volume. No counterpart in the reference: the same result
  * as vo_xor_volume, for callers that must not allocate device memory while
- * they run (code inside a stream host callback, services whose device memory
- * is owned by another allocator, hot loops kept off the allocator). It takes
+ * they run (services whose device memory is owned by another allocator, hot
+ * loops kept off the allocator). Call it from ordinary host code, not from a
+ * host function enqueued on a stream, where no CUDA call is allowed. It takes
  * no context: offs_a/z_a and offs_b/z_b are the device CSR arrays of two
- * volumes on `grid` (e.g. from vo_volume_device_ptrs), on the current device;
- * the work runs on `stream` (a cudaStream_t, NULL for the default stream),
- * which is synchronised before *volume is written.
+ * volumes on `grid` (e.g. from vo_volume_device_ptrs), all non-NULL, on the
+ * current device; the work runs on `stream` (a cudaStream_t of the current
+ * device, NULL for the default stream; another device's stream returns
+ * VO_EINVAL), which is synchronised before *volume is written.
  * Scratch is a fixed file-scope device array of 65537 doubles (512 KiB) that
  * every GPU loading the library keeps until exit; grids with more than
  * 16,777,216 columns (nx*ny) return VO_ERANGE. The first call on each device
- * looks up that array's device address, so make it before any stream capture.
+ * looks up that array's device address, so make it before any stream capture,
+ * and do not reset the device (cudaDeviceReset) after using this function.
  * All calls share the array: calls that overlap on the GPU (different streams
  * or threads) race and must be serialised by the caller. */
 int vo_xor_volume_noalloc(const vo_grid *grid, const int32_t *offs_a, const double *z_a,
@@ -227,28 +238,6 @@ int vo_sizer_train(vo_ctx *ctx, vo_sizer *s, const float *feats, const float *ta
 /* Attach (s != NULL) or detach (NULL) a sizer used by vo_morph_batched. The
  * context does not own it. */
 int vo_set_sizer(vo_ctx *ctx, vo_sizer *s);
-
-/* ---- host utilities (no device work) ---- */
-
-/* Seeded synthetic volume: union of spheres and flat-capped cylinders
- * evaluated at dexel centres, clipped to [0, zmax], merged per column. */
-typedef struct {
-  int32_t nx, ny;
-  double zmax;
-  int32_t n_spheres;
-  int32_t sphere_dist; /* 0: radius uniform in [s_rmin, s_rmax]; 1: lognormal(s_median, s_sigma) clipped */
-  double s_rmin, s_rmax, s_median, s_sigma;
-  int32_t n_cyl; /* endpoints uniform in the box, radius uniform in [c_rmin, c_rmax] */
-  double c_rmin, c_rmax;
-  uint64_t seed;
-} vo_synth_params;
-/* offs: caller array of nx*ny+1; *z is allocated (free with vo_host_free). */
-int vo_synth_volume(const vo_synth_params *p, int32_t *offs, double **z, int64_t *nseg);
-/* Watertight torus centred at (0.5,0.5,0.5), nu x nv quads split in triangles,
- * vertices displaced along the normal by uniform noise in [-noise, noise]. */
-int vo_synth_torus(int nu, int nv, double major, double minor, double noise, uint64_t seed,
-                   double **verts, int *nverts, int32_t **tris, int *ntris);
-void vo_host_free(void *p);
 
 #ifdef __cplusplus
 }

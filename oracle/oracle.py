@@ -24,7 +24,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libvo_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libvor3d_ref.so")
-REF_ROOT = os.environ.get("VO_REF_ROOT", "/root/reference")
+# the package's input generator built from the same source (make oracle), so that the CPU baseline
+# makes its inputs without loading a product library
+SYNTH_SO = os.path.join(HERE, "_build", "libvo_synth.so")
 
 OPS = {"dilation": 0, "erosion": 1, "opening": 2, "closing": 3}
 
@@ -70,10 +72,9 @@ class Grid:
 def build(ref: bool | None = None) -> None:
     """Builds the oracle (always) and the reference library (when its sources exist)."""
     subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
-    if ref is None:
-        ref = os.path.isdir(os.path.join(REF_ROOT, "src", "vor3d"))
-    if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_ROOT={REF_ROOT}"], check=True)
+    if ref is None or ref:
+        # build_ref.sh knows where the reference sources live and does nothing without them
+        subprocess.run(["sh", os.path.join(HERE, "build_ref.sh")], check=True)
 
 
 _lib = None
@@ -95,6 +96,7 @@ def lib():
         L.vo_or_get_volume.argtypes = [G, V]
         L.vo_or_get_volume.restype = C.c_double
         L.vo_or_dilate_columns.argtypes = [G, V, C.c_double, C.POINTER(C.c_int32), C.c_int, C.c_int, V]
+        L.vo_or_morph_columns.argtypes = [C.c_int, G, V, C.c_double, C.POINTER(C.c_int32), C.c_int, C.c_int, V]
         L.vo_or_pass1_pieces.argtypes = [G, V, C.c_double, C.c_int]
         L.vo_or_pass1_pieces.restype = C.c_int64
         L.vo_or_dexelize.argtypes = [C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_int32), C.c_int,
@@ -188,6 +190,20 @@ def dilate_columns(grid: Grid, offs, z, radius: float, cols, threads: int = 0):
                                 cols.ctypes.data_as(C.POINTER(C.c_int32)), int(cols.size),
                                 threads or os.cpu_count(), C.byref(cout))
     _rc(rc, "vo_or_dilate_columns")
+    return _csr_take(cout, int(cols.size))
+
+
+def morph_columns(grid: Grid, offs, z, radius: float, op: str, cols, threads: int = 0):
+    """Any op at the selected output columns only: returns (offs[len(cols)+1], z), equal to the
+    corresponding columns of morph(grid, offs, z, radius, op)."""
+    L = lib()
+    cols = np.ascontiguousarray(cols, dtype=np.int32)
+    cin, keep = _csr_in(offs, z)
+    cout = _Csr()
+    rc = L.vo_or_morph_columns(OPS[op], C.byref(grid.to_c()), C.byref(cin), float(radius),
+                               cols.ctypes.data_as(C.POINTER(C.c_int32)), int(cols.size),
+                               threads or os.cpu_count(), C.byref(cout))
+    _rc(rc, "vo_or_morph_columns")
     return _csr_take(cout, int(cols.size))
 
 

@@ -903,6 +903,136 @@ int vo_or_morph(int method, int op, const vo_or_grid *g, const vo_or_csr *in, do
   return rc;
 }
 
+/* --------------------------------------------------------------- selected columns of any op
+ *
+ * vo_or_morph_columns: the result of vo_or_morph (separable method) at selected
+ * columns only, with the same arithmetic, so that full-size GPU results can be
+ * checked exactly on a sample. Erosion complements the whole input (linear
+ * work, Voronoi.cpp:18-55), dilates the complement at the selected columns only
+ * and complements them back (Voronoi.cpp:57-89). Opening and closing evaluate
+ * their first op on the selected columns' lattice neighbourhoods (the only
+ * columns the second op reads) and their second op on the selected columns. */
+
+static int dilate_cols_norm(const vo_or_grid *g, const vo_or_csr *in, double radius, const int32_t *cols,
+                            int n, int nthreads, vo_or_csr *out) {
+  vo_or_csr norm = {0};
+  int nrc = normalize_inverted(g->nx * g->ny, in, &norm);
+  if (nrc < 0) return VO_OR_ENOMEM;
+  int rc = vo_or_dilate_columns(g, nrc > 0 ? &norm : in, radius, cols, n, nthreads, out);
+  free(norm.offs);
+  free(norm.z);
+  return rc;
+}
+
+static int erode_cols(const vo_or_grid *g, const vo_or_csr *in, double radius, const int32_t *cols, int n,
+                      int nthreads, vo_or_csr *out) {
+  const double zmin = g->origin[2] / g->spacing - 1;
+  const double zmax = g->origin[2] / g->spacing + 2 * g->padding + g->extent[2] / g->spacing + 1;
+  vo_or_csr neg = {0}, dil = {0};
+  int32_t *mcols = (int32_t *)malloc(sizeof(int32_t) * (size_t)(n > 0 ? n : 1));
+  int rc = mcols ? negate_grid(g->nx, g->ny, in, zmin, zmax, &neg) : VO_OR_ENOMEM;
+  if (rc) goto done;
+  for (int i = 0; i < n; ++i) mcols[i] = (cols[i] % g->nx + 1) + (g->nx + 2) * (cols[i] / g->nx + 1);
+  vo_or_grid g2 = *g;
+  g2.nx += 2;
+  g2.ny += 2;
+  rc = dilate_cols_norm(&g2, &neg, radius, mcols, n, nthreads, &dil);
+  if (rc) goto done;
+  if (csr_alloc(n, 2 * (int64_t)dil.offs[n] + 4 * (int64_t)n, out)) {
+    rc = VO_OR_ENOMEM;
+    goto done;
+  }
+  {
+    int64_t w = 0;
+    out->offs[0] = 0;
+    for (int i = 0; i < n; ++i) {
+      int k = negate_ray_range(dil.z + 2 * (size_t)dil.offs[i], 2 * (dil.offs[i + 1] - dil.offs[i]), zmin + 1,
+                               zmax - 1, out->z + w);
+      if (k % 2) {
+        rc = VO_OR_EINVAL;
+        goto done;
+      }
+      w += k;
+      out->offs[i + 1] = (int32_t)(w / 2);
+    }
+  }
+done:
+  free(mcols);
+  free(neg.offs);
+  free(neg.z);
+  free(dil.offs);
+  free(dil.z);
+  return rc;
+}
+
+/* Columns within the lattice reach (|dy| <= floor(R), |dx| <= floor(R)) of the
+ * selected ones, sorted and unique; *nb receives the count. */
+static int32_t *neighbourhood(const vo_or_grid *g, double radius, const int32_t *cols, int n, int *nb) {
+  const int D = (int)floor(radius), N = g->nx * g->ny;
+  unsigned char *mark = (unsigned char *)calloc((size_t)N, 1);
+  if (!mark) return NULL;
+  int cnt = 0;
+  for (int i = 0; i < n; ++i) {
+    const int cx = cols[i] % g->nx, cy = cols[i] / g->nx;
+    for (int y = cy - D; y <= cy + D; ++y)
+      for (int x = cx - D; x <= cx + D; ++x)
+        if (x >= 0 && x < g->nx && y >= 0 && y < g->ny && !mark[x + g->nx * y]) {
+          mark[x + g->nx * y] = 1;
+          ++cnt;
+        }
+  }
+  int32_t *out = (int32_t *)malloc(sizeof(int32_t) * (size_t)(cnt > 0 ? cnt : 1));
+  if (out) {
+    int k = 0;
+    for (int c = 0; c < N; ++c)
+      if (mark[c]) out[k++] = c;
+  }
+  free(mark);
+  *nb = cnt;
+  return out;
+}
+
+/* A full-grid CSR holding `part` (results at the sorted columns `sel`) and empty
+ * columns elsewhere. */
+static int scatter_cols(const vo_or_grid *g, const int32_t *sel, int n, const vo_or_csr *part, vo_or_csr *out) {
+  const int N = g->nx * g->ny;
+  if (csr_alloc(N, 2 * (int64_t)part->offs[n], out)) return VO_OR_ENOMEM;
+  memcpy(out->z, part->z, sizeof(double) * 2 * (size_t)part->offs[n]);
+  out->offs[0] = 0;
+  int k = 0;
+  for (int c = 0; c < N; ++c) {
+    if (k < n && sel[k] == c) ++k;
+    out->offs[c + 1] = part->offs[k];
+  }
+  return VO_OR_OK;
+}
+
+int vo_or_morph_columns(int op, const vo_or_grid *g, const vo_or_csr *in, double radius, const int32_t *cols,
+                        int ncols_sel, int nthreads, vo_or_csr *out) {
+  if (!g || !in || !cols || !out || ncols_sel < 0) return VO_OR_EINVAL;
+  for (int i = 0; i < ncols_sel; ++i)
+    if (cols[i] < 0 || cols[i] >= g->nx * g->ny) return VO_OR_EINVAL;
+  if (op == 0) return dilate_cols_norm(g, in, radius, cols, ncols_sel, nthreads, out);
+  if (op == 1) return erode_cols(g, in, radius, cols, ncols_sel, nthreads, out);
+  if (op != 2 && op != 3) return VO_OR_EINVAL;
+  int nb = 0;
+  int32_t *sel = neighbourhood(g, radius, cols, ncols_sel, &nb);
+  if (!sel) return VO_OR_ENOMEM;
+  vo_or_csr part = {0}, full = {0};
+  int rc = op == 2 ? erode_cols(g, in, radius, sel, nb, nthreads, &part)
+                   : dilate_cols_norm(g, in, radius, sel, nb, nthreads, &part);
+  if (!rc) rc = scatter_cols(g, sel, nb, &part, &full);
+  if (!rc)
+    rc = op == 2 ? dilate_cols_norm(g, &full, radius, cols, ncols_sel, nthreads, out)
+                 : erode_cols(g, &full, radius, cols, ncols_sel, nthreads, out);
+  free(sel);
+  free(part.offs);
+  free(part.z);
+  free(full.offs);
+  free(full.z);
+  return rc;
+}
+
 /* --------------------------------------------------------------- xor */
 
 static int union_segs(const double *a, int na2, const double *b, int nb2, double *out) {

@@ -43,6 +43,10 @@ int vo_or_dilate(const vo_or_grid *g, const vo_or_csr *in, double radius, int nt
 /* Separable dilation of selected output columns only (out CSR has ncols_sel+1 offsets). */
 int vo_or_dilate_columns(const vo_or_grid *g, const vo_or_csr *in, double radius, const int32_t *cols,
                          int ncols_sel, int nthreads, vo_or_csr *out);
+/* Any op (0 dilation, 1 erosion, 2 opening, 3 closing; separable method) at the
+ * selected output columns only (out CSR has ncols_sel+1 offsets). */
+int vo_or_morph_columns(int op, const vo_or_grid *g, const vo_or_csr *in, double radius, const int32_t *cols,
+                        int ncols_sel, int nthreads, vo_or_csr *out);
 /* Brute-force lattice-disc dilation (VoronoiBruteForce.cpp:16-100). */
 int vo_or_dilate_brute(const vo_or_grid *g, const vo_or_csr *in, double radius, int nthreads,
                        vo_or_csr *out);

@@ -14,9 +14,9 @@ import pytest
 from conftest import ROOT
 
 
-def header_functions():
+def header_functions(name: str | None = None):
     names = []
-    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+    for h in glob.glob(os.path.join(ROOT, "include", name or "*.h")):
         text = open(h).read()
         text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
         names += re.findall(r"\b(vo_[a-z0-9_]+)\s*\(", text)
@@ -31,16 +31,24 @@ def test_header_declares_the_boundary():
 
 
 def test_library_exports_every_declared_symbol(vo):
-    L = vo.lib()
-    missing = [n for n in header_functions() if not hasattr(L, n)]
-    assert not missing, f"symbols declared in include/*.h but not exported: {missing}"
+    # voroffset_gpu.h -> libvoroffset_gpu.so, voroffset_synth.h -> libvoroffset_synth.so
+    for header, L, path in (("voroffset_gpu.h", vo.lib(), vo.LIB_PATH),
+                            ("voroffset_synth.h", vo.synth_lib(), vo.SYNTH_LIB_PATH)):
+        missing = [n for n in header_functions(header) if not hasattr(L, n)]
+        assert not missing, f"symbols declared in {header} but not exported: {missing}"
+        out = os.popen(f"nm -D --defined-only {path}").read()
+        exported = set(re.findall(r" T (vo_[a-z0-9_]+)", out))
+        assert set(header_functions(header)) <= exported
+
+
+def test_gpu_library_holds_no_input_generator(vo):
     out = os.popen(f"nm -D --defined-only {vo.LIB_PATH}").read()
-    exported = set(re.findall(r" T (vo_[a-z0-9_]+)", out))
-    assert set(header_functions()) <= exported
+    assert "vo_synth_volume" not in out and "vo_synth_torus" not in out
 
 
 def test_python_mirror_covers_header(vo):
-    assert set(header_functions()) <= set(vo.SIGNATURES)
+    assert set(header_functions("voroffset_gpu.h")) <= set(vo.SIGNATURES)
+    assert set(header_functions("voroffset_synth.h")) <= set(vo.SYNTH_SIGNATURES)
 
 
 def test_synth_is_deterministic(vo):

@@ -105,3 +105,24 @@ def test_empty_volume(oracle):
     # erosion of nothing is nothing; the complement border keeps it empty
     o, zz = oracle.morph(g, offs, np.zeros(0), 3.0, "erosion")
     assert o[-1] == 0
+
+
+@pytest.mark.parametrize("op", OPS)
+@pytest.mark.parametrize("padded", [False, True])
+def test_morph_columns_equals_whole_volume(oracle, vo, op, padded):
+    """The selected-columns oracle (used to check full-size GPU results on a
+    sample) returns exactly the whole-volume result's columns, for every op,
+    at the grid edges too; on an unpadded grid the closing's complement leaves
+    [zmin, zmax] and produces inverted pairs, which it normalises the same way."""
+    g, offs, z = vo.synth_volume(vo.SynthSpec(56, ny=44, n_spheres=30, s_rmin=2, s_rmax=12, n_cyl=6, seed=61))
+    grid = ogrid(oracle, g)
+    if padded:
+        grid = oracle.Grid(g.nx, g.ny, (0.0, 0.0, -6.0), g.extent, 1.0, 3)
+    r = 5.5
+    want = oracle.morph(grid, offs, z, r, op)
+    rng = np.random.default_rng(5)
+    cols = np.unique(np.concatenate([rng.integers(0, g.ncols, 40), [0, g.nx - 1, g.ncols - 1]])).astype(np.int32)
+    so, sz = oracle.morph_columns(grid, offs, z, r, op, cols)
+    wo, wz = want
+    for i, c in enumerate(cols):
+        assert np.array_equal(sz[2 * so[i]:2 * so[i + 1]], wz[2 * wo[c]:2 * wo[c + 1]]), f"{op} column {c}"

@@ -111,6 +111,7 @@ SIGNATURES = {
                                    C.POINTER(_P), C.POINTER(_P), C.POINTER(_Timings)]),
     "vo_dexelize": (C.c_int, [_P, C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_int32), C.c_int,
                               C.POINTER(C.c_double), C.c_int, C.c_int, C.POINTER(_P)]),
+    "vo_dexelize_odd_columns": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "vo_xor_volume": (C.c_int, [_P, _P, _P, C.POINTER(C.c_double)]),
     "vo_xor_volume_noalloc": (C.c_int, [C.POINTER(_Grid), _P, _P, _P, _P, _P, C.POINTER(C.c_double)]),
     "vo_batch_create": (C.c_int, [_P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_int,
@@ -132,6 +133,12 @@ SIGNATURES = {
     "vo_sizer_train": (C.c_int, [_P, _P, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int, C.c_int,
                                  C.c_float, C.POINTER(C.c_float)]),
     "vo_set_sizer": (C.c_int, [_P, _P]),
+}
+
+# Every function of include/voroffset_synth.h (the host-only input generator,
+# libvoroffset_synth.so) with its ctypes signature.
+SYNTH_LIB_PATH = os.path.join(PKG, "libvoroffset_synth.so")
+SYNTH_SIGNATURES = {
     "vo_synth_volume": (C.c_int, [C.POINTER(_SynthParams), C.POINTER(C.c_int32),
                                   C.POINTER(C.POINTER(C.c_double)), C.POINTER(C.c_int64)]),
     "vo_synth_torus": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_uint64,
@@ -139,6 +146,22 @@ SIGNATURES = {
                                  C.POINTER(C.POINTER(C.c_int32)), C.POINTER(C.c_int)]),
     "vo_host_free": (None, [_P]),
 }
+_synth = {}
+
+
+def synth_lib(path: str | None = None) -> C.CDLL:
+    """Loads the input generator: libvoroffset_synth.so, or the same source built at `path`."""
+    path = path or SYNTH_LIB_PATH
+    if path not in _synth:
+        if not os.path.exists(path):
+            raise RuntimeError(f"{path} is missing: run `python -m voroffset_gb300.build`")
+        L = C.CDLL(path)
+        for name, (res, args) in SYNTH_SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _synth[path] = L
+    return _synth[path]
 
 
 def lib(build_if_missing: bool = False) -> C.CDLL:
@@ -308,6 +331,12 @@ class Context:
                     "vo_dexelize")
         return Volume(self, out.value)
 
+    def dexelize_odd_columns(self) -> int:
+        """Columns of the last dexelize whose ray met the mesh an odd number of times (last hit dropped)."""
+        n = C.c_int64()
+        self._check(lib().vo_dexelize_odd_columns(self.handle, C.byref(n)), "vo_dexelize_odd_columns")
+        return int(n.value)
+
     def xor_volume(self, a: Volume, b: Volume) -> float:
         r = C.c_double()
         self._check(lib().vo_xor_volume(self.handle, a.handle, b.handle, C.byref(r)), "vo_xor_volume")
@@ -448,8 +477,9 @@ class SynthSpec:
     ny: int | None = None
 
 
-def synth_volume(spec: SynthSpec):
-    """Returns (Grid, offs, z) with spacing 1, origin 0, padding 0, extent (nx, ny, zmax)."""
+def synth_volume(spec: SynthSpec, synth: str | None = None):
+    """Returns (Grid, offs, z) with spacing 1, origin 0, padding 0, extent (nx, ny, zmax).
+    `synth`: path of another build of the generator (default libvoroffset_synth.so)."""
     nx = int(spec.n)
     ny = int(spec.ny or spec.n)
     zmax = float(spec.zmax if spec.zmax is not None else spec.n)
@@ -459,12 +489,13 @@ def synth_volume(spec: SynthSpec):
     offs = np.zeros(nx * ny + 1, dtype=np.int32)
     pz = C.POINTER(C.c_double)()
     ns = C.c_int64()
-    rc = lib().vo_synth_volume(C.byref(p), _i32p(offs), C.byref(pz), C.byref(ns))
+    L = synth_lib(synth)
+    rc = L.vo_synth_volume(C.byref(p), _i32p(offs), C.byref(pz), C.byref(ns))
     if rc != VO_OK:
         raise GpuError(rc, "vo_synth_volume")
     n2 = 2 * int(ns.value)
     z = np.ctypeslib.as_array(pz, shape=(max(n2, 1),))[:n2].copy()
-    lib().vo_host_free(C.cast(pz, C.c_void_p))
+    L.vo_host_free(C.cast(pz, C.c_void_p))
     grid = Grid(nx, ny, (0.0, 0.0, 0.0), (float(nx), float(ny), zmax), 1.0, 0)
     return grid, offs, z
 
@@ -474,26 +505,31 @@ def synth_torus(nu: int = 256, nv: int = 64, major: float = 0.30, minor: float =
     pv = C.POINTER(C.c_double)()
     pt = C.POINTER(C.c_int32)()
     nvv, ntt = C.c_int(), C.c_int()
-    rc = lib().vo_synth_torus(nu, nv, major, minor, noise, seed, C.byref(pv), C.byref(nvv), C.byref(pt),
-                              C.byref(ntt))
+    L = synth_lib()
+    rc = L.vo_synth_torus(nu, nv, major, minor, noise, seed, C.byref(pv), C.byref(nvv), C.byref(pt),
+                          C.byref(ntt))
     if rc != VO_OK:
         raise GpuError(rc, "vo_synth_torus")
     verts = np.ctypeslib.as_array(pv, shape=(3 * nvv.value,)).copy().reshape(-1, 3)
     tris = np.ctypeslib.as_array(pt, shape=(3 * ntt.value,)).copy().reshape(-1, 3)
-    lib().vo_host_free(C.cast(pv, C.c_void_p))
-    lib().vo_host_free(C.cast(pt, C.c_void_p))
+    L.vo_host_free(C.cast(pv, C.c_void_p))
+    L.vo_host_free(C.cast(pt, C.c_void_p))
     return verts, tris
 
 
 # Named workloads of the benchmark configurations (sizes and distributions).
-def workload(name: str, seed: int = 1):
-    """Synthetic volume for a named configuration: returns (Grid, offs, z)."""
+def workload_spec(name: str, seed: int = 1) -> SynthSpec:
+    """Generator parameters of a named configuration."""
     if name == "spheres1024":
-        return synth_volume(SynthSpec(1024, n_spheres=4096, s_rmin=4, s_rmax=40, seed=seed))
+        return SynthSpec(1024, n_spheres=4096, s_rmin=4, s_rmax=40, seed=seed)
     if name == "spheres_cyl2048":
-        return synth_volume(SynthSpec(2048, n_spheres=16384, sphere_dist="lognormal", s_median=12,
-                                      s_sigma=0.5, s_rmin=2, s_rmax=80, n_cyl=2000, c_rmin=1, c_rmax=4,
-                                      seed=seed))
+        return SynthSpec(2048, n_spheres=16384, sphere_dist="lognormal", s_median=12, s_sigma=0.5, s_rmin=2,
+                         s_rmax=80, n_cyl=2000, c_rmin=1, c_rmax=4, seed=seed)
     if name == "cyl4096":
-        return synth_volume(SynthSpec(4096, n_cyl=20000, c_rmin=1.5, c_rmax=3.0, seed=seed))
+        return SynthSpec(4096, n_cyl=20000, c_rmin=1.5, c_rmax=3.0, seed=seed)
     raise KeyError(name)
+
+
+def workload(name: str, seed: int = 1, synth: str | None = None):
+    """Synthetic volume for a named configuration: returns (Grid, offs, z)."""
+    return synth_volume(workload_spec(name, seed), synth)

@@ -1,4 +1,5 @@
-"""Builds libvoroffset_gpu.so in-tree for sm_103a.
+"""Builds libvoroffset_gpu.so (and the host-only input generator
+libvoroffset_synth.so) in-tree for sm_103a.
 
 Every CUDA translation unit is compiled with
 ``nvcc -gencode arch=compute_103a,code=sm_103a -lineinfo -O3`` in parallel,
@@ -25,6 +26,8 @@ BIN = os.path.join(PKG, "bin")
 BUILD = os.path.join(PKG, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 LIB = os.path.join(PKG, "libvoroffset_gpu.so")
+SYNTH_SRC = os.path.join(PKG, "synth", "vo_synth.cpp")
+SYNTH_LIB = os.path.join(PKG, "libvoroffset_synth.so")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 
@@ -89,6 +92,12 @@ def build(force: bool = False, verbose: bool = False) -> str:
         tmp = LIB + ".tmp"
         _compile([nvcc, ARCH, "-shared", "-o", tmp] + objs + ["-lpthread"], verbose)
         os.replace(tmp, LIB)
+    # host-only input generator, a library of its own (no device code, not part of the GPU library)
+    if not os.path.exists(SYNTH_LIB) or os.path.getmtime(SYNTH_LIB) < max(os.path.getmtime(SYNTH_SRC), hdr_time):
+        tmp = SYNTH_LIB + ".tmp"
+        _compile(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-pthread", f"-I{INCLUDE}",
+                  SYNTH_SRC, "-o", tmp], verbose)
+        os.replace(tmp, SYNTH_LIB)
     cli = os.path.join(BIN, "offset3d_gpu")
     cli_src = os.path.join(HOST, "offset3d_gpu.cpp")
     if not os.path.exists(cli) or os.path.getmtime(cli) < max(os.path.getmtime(LIB), os.path.getmtime(cli_src)):

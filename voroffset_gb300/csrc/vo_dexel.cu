@@ -113,7 +113,8 @@ __global__ void k_bin_fill(Mesh m, GridView g, const int32_t *boffs, int32_t *cu
     }
 }
 
-// Returns the number of (paired) values of column c, or -1 on overflow.
+// Returns the number of hits of column c (the FILL pass writes the first
+// 2 * (hits / 2) of them: an unpaired trailing hit is dropped), or -1 on overflow.
 template <bool FILL>
 __device__ int cast_column(const Mesh &m, const GridView &g, const int32_t *boffs, const int32_t *bins,
                            int c, double *hits, int cap, double *out) {
@@ -141,10 +142,11 @@ __device__ int cast_column(const Mesh &m, const GridView &g, const int32_t *boff
       hits[i] = v;
     }
   }
+  const int raw = nh;
   nh &= ~1;  // an unpaired trailing hit is ignored (values are consumed in pairs)
   if (FILL)
     for (int i = 0; i < nh; ++i) out[i] = hits[i];
-  return nh;
+  return raw;
 }
 
 template <bool FILL>
@@ -161,6 +163,7 @@ __global__ void k_cast(Mesh m, GridView g, const int32_t *boffs, const int32_t *
       counts[c] = 0;
     } else {
       counts[c] = n / 2;
+      if (n & 1) atomicAdd(ovf_count + 2, 1);  // odd columns (the flag word after the two status words)
     }
   }
 }
@@ -176,7 +179,10 @@ __global__ void k_cast_big(Mesh m, GridView g, const int32_t *boffs, const int32
     const int n = cast_column<FILL>(m, g, boffs, bins, c, hits, kHitCapBig,
                                     FILL ? oz + 2 * (size_t)ooffs[c] : nullptr);
     if (n < 0) *fatal = 1;
-    if (!FILL) counts[c] = n < 0 ? 0 : n / 2;
+    if (!FILL) {
+      counts[c] = n < 0 ? 0 : n / 2;
+      if (n > 0 && (n & 1)) atomicAdd(fatal + 1, 1);  // odd columns, as in k_cast
+    }
   }
 }
 
@@ -184,6 +190,13 @@ __global__ void k_cast_big(Mesh m, GridView g, const int32_t *boffs, const int32
 }  // namespace vo
 
 using namespace vo;
+
+extern "C" int vo_dexelize_odd_columns(vo_ctx *ctx, int64_t *count) {
+  if (!ctx || !count) return VO_EINVAL;
+  if (ctx->dexel_odd_columns < 0) return set_error(ctx, VO_EINVAL, "no successful vo_dexelize on this context");
+  *count = ctx->dexel_odd_columns;
+  return VO_OK;
+}
 
 extern "C" int vo_dexelize(vo_ctx *ctx, const double *verts, int nv, const int32_t *tris, int nt,
                            double *spacing, int padding, int num_dexels, vo_volume **out) {
@@ -194,6 +207,7 @@ extern "C" int vo_dexelize(vo_ctx *ctx, const double *verts, int nv, const int32
     if (tris[i] < 0 || tris[i] >= nv) return set_error(ctx, VO_EINVAL, "dexelize: vertex index out of range");
   cudaSetDevice(ctx->device);
   ctx->err.clear();
+  ctx->dexel_odd_columns = -1;
   *out = nullptr;
   // create_dexels (Dexelize.cpp:254-271)
   double mn[3], mx[3];
@@ -241,7 +255,7 @@ extern "C" int vo_dexelize(vo_ctx *ctx, const double *verts, int nv, const int32
     if (nt) cudaMemcpyAsync(df, tris, sizeof(int32_t) * 3 * (size_t)nt, cudaMemcpyHostToDevice, ctx->stream);
     cudaMemsetAsync(cnt, 0, sizeof(int32_t) * ncols, ctx->stream);
     cudaMemsetAsync(cursor, 0, sizeof(int32_t) * ncols, ctx->stream);
-    cudaMemsetAsync(ctx->d_flags, 0, 2 * sizeof(int), ctx->stream);
+    cudaMemsetAsync(ctx->d_flags, 0, 3 * sizeof(int), ctx->stream);  // overflow count, fatal, odd columns
     if (nt) k_bin_count<<<(nt + 127) / 128, 128, 0, ctx->stream>>>(m, gv, cnt);
     rc = scan_counts(ctx, cnt, boffs, ncols, &nb);
   }
@@ -264,13 +278,15 @@ extern "C" int vo_dexelize(vo_ctx *ctx, const double *verts, int nv, const int32
                                                                (double *)res->z, ctx->d_flags, ovf_cols);
     k_cast_big<true><<<gbig, 32, 0, ctx->stream>>>(m, gv, boffs, bins, nullptr, res->offs, (double *)res->z,
                                                    ctx->d_flags, ovf_cols, big, ctx->d_flags + 1);
-    int hf[2] = {0, 0};
+    int hf[3] = {0, 0, 0};
     cudaMemcpyAsync(hf, ctx->d_flags, sizeof(hf), cudaMemcpyDeviceToHost, ctx->stream);
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess)
       rc = cuda_error(ctx, e, "dexelize");
     else if (hf[1])
       rc = set_error(ctx, VO_EINTERNAL, "dexelize: a column has more than 4096 hits");
+    else
+      ctx->dexel_odd_columns = hf[2];
   }
   dfree(ctx, dv);
   dfree(ctx, df);

@@ -27,10 +27,12 @@
 // not cover, and is skipped. Both bounds are computed with directed rounding,
 // so skipping never changes the union.
 //
-// Capacities: the main kernels keep kUnionCap (32) intervals per column;
-// columns that need more are re-run by the same code with kUnionCapMid (128)
-// intervals (count, then fill), and beyond that by an FP64 kernel with a large
-// working list in global scratch.
+// Capacities: the main kernels keep KA union slots per column (KA in
+// {24, 32, 48, 64}, chosen per input density or by the batch autotuner; one
+// slot holds the sentinel, so KA - 1 intervals); columns that need more are
+// re-run by the same code with kUnionCapMid (128) slots (count, then fill),
+// and beyond that by an FP64 kernel with a large working list in global
+// scratch.
 #include <algorithm>
 #include <chrono>
 #include <cmath>

@@ -97,6 +97,7 @@ struct vo_ctx {
   long long *d_total = nullptr;
   long long *h_total = nullptr;  // pinned
   vo_sizer *sizer = nullptr;     // learned sizing for the batched executor (not owned)
+  int64_t dexel_odd_columns = -1;  // odd-hit columns of the last vo_dexelize (-1: none yet)
   std::vector<std::pair<long long, int>> tune_cache;  // batch autotuner: shape key -> rows per block
 };
 

@@ -6,6 +6,9 @@
 //   -x operation, -f force overwrite, -u radius in mm.
 // Methods: gpu (FP32-guarded exact, default), gpu_separable (FP64 kernels),
 // gpu_brute (lattice-disc brute force).
+// Additions: -s/--save-volume FILE writes the output volume (the text format of
+// CompressedVolume::save, or the exact binary CSR dump when FILE ends in .csr);
+// --boxes writes six quads per dexel box instead of the boundary surface.
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -22,6 +25,8 @@ namespace {
 
 struct Args {
   std::string input, output_mesh = "output.obj", output_json, method = "gpu", operation = "dilation";
+  std::string save_volume;
+  bool boxes = false;
   double radius = 8, dexels_size = 1;
   int padding = 0, num_dexels = 256, num_thread = 1;
   bool force = false, radius_in_mm = false;
@@ -31,7 +36,7 @@ struct Args {
   std::fprintf(stderr,
                "%s\nusage: offset3d_gpu input [-o out.obj] [-j out.json] [-d size] [-n num_dexels] [-p padding]\n"
                "       [-r radius] [-m gpu|gpu_separable|gpu_brute] [-x noop|dilation|erosion|closing|opening]\n"
-               "       [-f] [-u]\n",
+               "       [-f] [-u] [-s volume.txt|volume.csr] [--boxes]\n",
                msg);
   std::exit(2);
 }
@@ -56,6 +61,8 @@ Args parse(int argc, char **argv) {
     else if (s == "-x" || s == "--apply") a.operation = val("-x");
     else if (s == "-f" || s == "--force") a.force = true;
     else if (s == "-u" || s == "--radius_in_mm") a.radius_in_mm = true;
+    else if (s == "-s" || s == "--save-volume") a.save_volume = val("-s");
+    else if (s == "--boxes") a.boxes = true;
     else if (!s.empty() && s[0] != '-' && a.input.empty()) a.input = s;
     else if (!s.empty() && s[0] != '-') a.output_mesh = s;
     else usage(("unknown option " + s).c_str());
@@ -99,8 +106,20 @@ int main(int argc, char **argv) {
     if (!args.output_mesh.empty()) {
       if (exists(args.output_mesh) && !args.force)
         std::fprintf(stderr, "Output mesh already exists. Please use -f to force overwriting.\n");
+      else if (args.boxes)
+        dexel_dump_boxes(args.output_mesh, output);
       else
         dexel_dump(args.output_mesh, output);
+    }
+    if (!args.save_volume.empty()) {
+      const std::string &f = args.save_volume;
+      if (f.size() >= 4 && f.compare(f.size() - 4, 4, ".csr") == 0) {
+        output.save_csr(f);
+      } else {
+        std::ofstream vo(f);
+        vo.precision(17);
+        output.save(vo);
+      }
     }
     const double total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     if (!args.output_json.empty()) {

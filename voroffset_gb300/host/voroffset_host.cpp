@@ -3,9 +3,11 @@
 
 #include <cmath>
 #include <cstdio>
+#include <cstring>
 #include <fstream>
 #include <iostream>
 #include <sstream>
+#include <unordered_map>
 
 namespace voroffset3d {
 
@@ -91,6 +93,60 @@ void CompressedVolume::load(std::istream &in) {
     for (auto &v : row) in >> v;
   }
   if (!in) throw std::runtime_error("CompressedVolume::load: truncated");
+}
+
+namespace {
+constexpr char kCsrMagic[8] = {'V', 'O', 'C', 'S', 'R', '0', '0', '1'};
+}
+
+void CompressedVolume::save_csr(const std::string &filename) const {
+  std::vector<int32_t> offs;
+  std::vector<double> z;
+  to_csr(offs, z);
+  std::ofstream out(filename, std::ios::binary);
+  if (!out) throw std::runtime_error("cannot write " + filename);
+  const int32_t head[3] = {nx_, ny_, padding_};
+  const double geo[7] = {origin_[0], origin_[1], origin_[2], extent_[0], extent_[1], extent_[2], spacing_};
+  const int64_t nseg = (int64_t)z.size() / 2;
+  out.write(kCsrMagic, 8);
+  out.write(reinterpret_cast<const char *>(head), sizeof head);
+  out.write(reinterpret_cast<const char *>(geo), sizeof geo);
+  out.write(reinterpret_cast<const char *>(&nseg), sizeof nseg);
+  out.write(reinterpret_cast<const char *>(offs.data()), (std::streamsize)(sizeof(int32_t) * offs.size()));
+  out.write(reinterpret_cast<const char *>(z.data()), (std::streamsize)(sizeof(double) * z.size()));
+  if (!out) throw std::runtime_error("write failed: " + filename);
+}
+
+void CompressedVolume::load_csr(const std::string &filename) {
+  std::ifstream in(filename, std::ios::binary);
+  if (!in) throw std::runtime_error("cannot open " + filename);
+  char magic[8];
+  int32_t head[3];
+  double geo[7];
+  int64_t nseg = 0;
+  in.read(magic, 8);
+  in.read(reinterpret_cast<char *>(head), sizeof head);
+  in.read(reinterpret_cast<char *>(geo), sizeof geo);
+  in.read(reinterpret_cast<char *>(&nseg), sizeof nseg);
+  if (!in || std::memcmp(magic, kCsrMagic, 8) != 0 || head[0] < 0 || head[1] < 0 || nseg < 0)
+    throw std::runtime_error("not a CSR volume: " + filename);
+  vo_grid g;
+  g.nx = head[0];
+  g.ny = head[1];
+  g.padding = head[2];
+  for (int k = 0; k < 3; ++k) {
+    g.origin[k] = geo[k];
+    g.extent[k] = geo[3 + k];
+  }
+  g.spacing = geo[6];
+  std::vector<int32_t> offs((size_t)g.nx * g.ny + 1);
+  std::vector<double> z(2 * (size_t)nseg);
+  in.read(reinterpret_cast<char *>(offs.data()), (std::streamsize)(sizeof(int32_t) * offs.size()));
+  in.read(reinterpret_cast<char *>(z.data()), (std::streamsize)(sizeof(double) * z.size()));
+  if (!in || offs[0] != 0 || offs.back() != nseg) throw std::runtime_error("truncated CSR volume: " + filename);
+  for (size_t c = 0; c + 1 < offs.size(); ++c)
+    if (offs[c + 1] < offs[c]) throw std::runtime_error("bad CSR offsets: " + filename);
+  from_csr(g, offs.data(), z.data());
 }
 
 vo_grid CompressedVolume::grid() const {
@@ -278,6 +334,60 @@ CompressedVolume create_dexels(VoronoiMorphoGpu &gpu, const std::string &filenam
   return out;
 }
 
+namespace {
+
+// Closed intervals of column list a minus those of b (both sorted, disjoint;
+// flat [z0, z1, z2, z3, ...]); pieces of zero length are dropped.
+std::vector<double> interval_minus(const std::vector<double> &a, const std::vector<double> *b) {
+  std::vector<double> out;
+  for (size_t i = 0; i + 1 < a.size(); i += 2) {
+    double lo = a[i];
+    const double hi = a[i + 1];
+    if (b)
+      for (size_t j = 0; j + 1 < b->size() && lo < hi; j += 2) {
+        const double blo = (*b)[j], bhi = (*b)[j + 1];
+        if (bhi <= lo) continue;
+        if (blo >= hi) break;
+        if (blo > lo) {
+          out.push_back(lo);
+          out.push_back(blo);
+        }
+        lo = bhi;
+      }
+    if (lo < hi) {
+      out.push_back(lo);
+      out.push_back(hi);
+    }
+  }
+  return out;
+}
+
+// OBJ writer with vertices merged by (lattice x, lattice y, z).
+struct ObjWriter {
+  std::ostream &out;
+  double ox, oy, h;
+  std::unordered_map<std::string, size_t> ids;
+  std::vector<std::array<size_t, 4>> faces;
+  size_t next = 1;
+  size_t vertex(int ix, int iy, double z) {
+    char key[64];
+    uint64_t zb;
+    std::memcpy(&zb, &z, sizeof zb);
+    std::snprintf(key, sizeof key, "%d:%d:%llx", ix, iy, (unsigned long long)zb);
+    auto it = ids.find(key);
+    if (it != ids.end()) return it->second;
+    out << "v " << ox + ix * h << ' ' << oy + iy * h << ' ' << z * h << "\n";
+    ids.emplace(key, next);
+    return next++;
+  }
+  void quad(size_t a, size_t b, size_t c, size_t d) { faces.push_back({a, b, c, d}); }
+  void finish() {
+    for (const auto &f : faces) out << "f " << f[0] << ' ' << f[1] << ' ' << f[2] << ' ' << f[3] << "\n";
+  }
+};
+
+}  // namespace
+
 void dexel_dump(const std::string &filename, const CompressedVolume &dexels) {
   std::ofstream out(filename);
   if (!out) throw std::runtime_error("cannot write " + filename);
@@ -295,6 +405,49 @@ void dexel_dump(const std::string &filename, const CompressedVolume &dexels) {
       }
     return;
   }
+  ObjWriter w{out, o[0], o[1], h, {}, {}, 1};
+  for (int y = 0; y < gs[1]; ++y)
+    for (int x = 0; x < gs[0]; ++x) {
+      const auto &c = dexels.at(x, y);
+      // bottom and top faces; a face shared by two touching segments is interior
+      for (size_t i = 0; i + 1 < c.size(); i += 2) {
+        const double z0 = c[i], z1 = c[i + 1];
+        if (!(i >= 2 && c[i - 1] == z0))
+          w.quad(w.vertex(x, y, z0), w.vertex(x, y + 1, z0), w.vertex(x + 1, y + 1, z0), w.vertex(x + 1, y, z0));
+        if (!(i + 2 < c.size() && c[i + 2] == z1))
+          w.quad(w.vertex(x, y, z1), w.vertex(x + 1, y, z1), w.vertex(x + 1, y + 1, z1), w.vertex(x, y + 1, z1));
+      }
+      // sides: the column's intervals minus the neighbour's, facing the neighbour
+      const std::vector<double> *nb[4] = {
+          x > 0 ? &dexels.at(x - 1, y) : nullptr, x + 1 < gs[0] ? &dexels.at(x + 1, y) : nullptr,
+          y > 0 ? &dexels.at(x, y - 1) : nullptr, y + 1 < gs[1] ? &dexels.at(x, y + 1) : nullptr};
+      for (int s = 0; s < 4; ++s) {
+        const std::vector<double> open = interval_minus(c, nb[s]);
+        for (size_t i = 0; i + 1 < open.size(); i += 2) {
+          const double z0 = open[i], z1 = open[i + 1];
+          if (s == 0)
+            w.quad(w.vertex(x, y, z0), w.vertex(x, y, z1), w.vertex(x, y + 1, z1), w.vertex(x, y + 1, z0));
+          else if (s == 1)
+            w.quad(w.vertex(x + 1, y, z0), w.vertex(x + 1, y + 1, z0), w.vertex(x + 1, y + 1, z1),
+                   w.vertex(x + 1, y, z1));
+          else if (s == 2)
+            w.quad(w.vertex(x, y, z0), w.vertex(x + 1, y, z0), w.vertex(x + 1, y, z1), w.vertex(x, y, z1));
+          else
+            w.quad(w.vertex(x, y + 1, z0), w.vertex(x, y + 1, z1), w.vertex(x + 1, y + 1, z1),
+                   w.vertex(x + 1, y + 1, z0));
+        }
+      }
+    }
+  w.finish();
+}
+
+void dexel_dump_boxes(const std::string &filename, const CompressedVolume &dexels) {
+  std::ofstream out(filename);
+  if (!out) throw std::runtime_error("cannot write " + filename);
+  out.precision(17);
+  const auto gs = dexels.gridSize();
+  const auto o = dexels.origin();
+  const double h = dexels.spacing();
   // one box per segment (Dexelize.cpp:320-343), written as six quads each
   size_t base = 1;
   for (int y = 0; y < gs[1]; ++y)

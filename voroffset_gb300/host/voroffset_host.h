@@ -51,6 +51,12 @@ class CompressedVolume {
   // Text marshalling (CompressedVolume.cpp:116-152).
   void save(std::ostream &out) const;
   void load(std::istream &in);
+  // Binary CSR dump (no reference counterpart; exact, for golden files and
+  // large volumes): "VOCSR001", int32 nx, ny, padding, FP64 origin[3],
+  // extent[3], spacing, int64 segment count, int32 offsets[nx*ny+1], FP64
+  // endpoint pairs, all little-endian.
+  void save_csr(const std::string &filename) const;
+  void load_csr(const std::string &filename);
 
   // CSR packing for the C ABI.
   vo_grid grid() const;
@@ -114,9 +120,16 @@ TriMesh load_mesh(const std::string &filename);  // .obj or .off
 CompressedVolume create_dexels(VoronoiMorphoGpu &gpu, const std::string &filename, double &voxel_size,
                                int padding = 0, int num_voxels = -1);
 
-// dexel_dump (Dexelize.cpp:281-351): one box per segment. ".xyz" writes the
-// segment endpoints at the dexel centres; otherwise a Wavefront OBJ with the
-// six faces of every box is written.
+// dexel_dump (Dexelize.cpp:281-351): the dexel boxes of a volume, one per
+// segment. ".xyz" writes the segment endpoints at the dexel centres
+// (points_dump). Otherwise a Wavefront OBJ of the boxes' boundary: the faces
+// no neighbouring box covers (top and bottom of every segment, and each side
+// minus the neighbouring column's segments there), with vertices merged, the
+// effect of compute_borders / connect / remove_isolated on the box cells.
+// Side faces are split only at the z values of the two columns they separate,
+// so vertices of other columns may lie on their edges (T-junctions).
 void dexel_dump(const std::string &filename, const CompressedVolume &dexels);
+// The six faces of every box, eight unshared vertices per box.
+void dexel_dump_boxes(const std::string &filename, const CompressedVolume &dexels);
 
 }  // namespace voroffset3d

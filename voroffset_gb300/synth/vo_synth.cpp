@@ -17,7 +17,7 @@
 #include <thread>
 #include <vector>
 
-#include "voroffset_gpu.h"
+#include "voroffset_synth.h"
 
 namespace {
 
