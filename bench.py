@@ -11,7 +11,8 @@ pairs) is larger than L2 (129 MB), so no flush is needed between steps.
           is the batch plan (vo_batch_*) with the learned sizer: one step is a
           replay of the captured graph plus the conversion of the output slots
           to CSR. The plan is built once before the warm-up.
-  arms  : the plain GPU method (FP64 separable, count then fill) and the
+  arms  : the plain GPU method (the separable scheme's envelope sweeps in
+          FP64), its painter form (FP64, count then fill) and the
           single-volume FP32-guarded method on the same volume, for the
           "plain vs batched+learned" comparison.
   e2e   : the same metric through the C ABI from pinned host buffers: upload,
@@ -51,7 +52,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--method", default="batched", choices=["batched", "separable", "brute", "fast"],
+    ap.add_argument("--method", default="batched", choices=["batched", "separable", "brute", "fast", "envelope"],
                     help="batched: a captured batch plan with the learned sizer (the headline)")
     ap.add_argument("--no-sizer", action="store_true", help="batched plan without the learned sizer")
     ap.add_argument("--no-arms", action="store_true", help="skip the plain / single-volume comparison arms")
@@ -452,6 +453,8 @@ def main():
             out, t = ctx.morph(vin, "dilation", args.radius, method)
             acc["launches"] += t["kernel_launches"]
             acc["kernel_ms"] += max(t["kernel_ms"])
+            acc["pass1_ms"] = acc.get("pass1_ms", 0.0) + t["pass1_ms"]
+            acc["pass2_ms"] = acc.get("pass2_ms", 0.0) + t["pass2_ms"]
             acc["out_segs"] = out.nseg
             acc["mid"] = t["mid_pieces"]
             out.free()
@@ -486,12 +489,19 @@ def main():
     # (FP64 separable, count then fill) and the single-volume FP32-guarded method
     arms = {}
     if args.method == "batched" and not args.no_arms:
-        for name, method, k in (("plain_separable_fp64", "separable", max(1, args.steps // 2)),
+        # the plain method is the separable scheme's sweeping envelope form in FP64; the painter form
+        # (per-column pass-1 pieces, then their union) is the other FP64 arm
+        for name, method, k in (("plain_envelope_fp64", "envelope", args.steps),
+                                ("painter_separable_fp64", "separable", max(1, args.steps // 2)),
                                 ("fast_single_volume", "fast", args.steps)):
-            ms = timed(single_step(method), k, 1)
+            ms = timed(single_step(method), k, 1, after_warmup=lambda: acc.update(pass1_ms=0.0, pass2_ms=0.0))
             arms[name] = {"value": world * ncols * k / (ms / 1e3) / 1e6, "unit": "Mcolumns/s",
                           "ms_per_step": ms / k, "steps": k}
-        arms["batched_vs_plain"] = value / arms["plain_separable_fp64"]["value"]
+            if method == "envelope":
+                arms[name]["pass1_ms"] = acc.get("pass1_ms", 0.0) / k
+                arms[name]["pass2_ms"] = acc.get("pass2_ms", 0.0) / k
+        arms["batched_vs_plain"] = value / arms["plain_envelope_fp64"]["value"]
+        arms["batched_vs_painter"] = value / arms["painter_separable_fp64"]["value"]
 
     # ---------------- end-to-end arm (pinned host buffers through the C ABI)
     pin_offs = torch.empty(offs.size, dtype=torch.int32, pin_memory=True).numpy()
@@ -525,7 +535,8 @@ def main():
     e2e = job_rate(world, ncols * args.steps, e2e_s)
 
     # ---------------- roofline of the dominant kernel
-    kname = {"batched": "k_fast_batched", "fast": "k_fast", "separable": "k_pass2", "brute": "k_brute"}[args.method]
+    kname = {"batched": "k_fast_batched", "fast": "k_fast", "separable": "k_pass2", "brute": "k_brute",
+             "envelope": "k_env2"}[args.method]
     per_launch = kernel_ms / args.steps
     alg_bytes = 4 * (ncols + 1) + 16 * int(offs[-1]) + 4 * (ncols + 1) + 16 * int(out_segs)
     peak, peak_kind = peaks()
@@ -537,7 +548,7 @@ def main():
                 "algorithmic_bytes": alg_bytes,
                 "op_achieved": alg_bytes / (dev_ms / args.steps / 1e3) / 1e9}
 
-    dtype = "f64" if args.method in ("separable", "brute") else "f32+f64"
+    dtype = "f64" if args.method in ("separable", "brute", "envelope") else "f32+f64"
     cfg = bench_config(args, grid, offs)
     run = {"method": args.method if args.method != "batched" else "batched+learned" if sizer else "batched",
            "out_segments": int(out_segs), "mid_pieces": int(mid),

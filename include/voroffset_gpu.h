@@ -55,10 +55,17 @@ extern "C" {
  *   the in-GPU cross-check.
  * VO_METHOD_FAST: the separable scheme with FP32 envelope arithmetic guarded by
  *   FP64 re-evaluation of near-tie merge/touch decisions (no reference
- *   counterpart). */
+ *   counterpart).
+ * VO_METHOD_ENVELOPE: the separable scheme as the reference sweeps it, FP64:
+ *   pass 1 sweeps each x-line keeping the half-space Voronoi envelope of the
+ *   segments (Voronoi2D.cpp:591-723), pass 2 sweeps each row keeping the live
+ *   stadiums of the pass-1 pieces and takes their union on every line
+ *   (SeparatePower2D.cpp:228-541), one warp per line / one block per row.
+ *   Same results as VO_METHOD_SEPARABLE. */
 #define VO_METHOD_SEPARABLE 0
 #define VO_METHOD_BRUTE 1
 #define VO_METHOD_FAST 2
+#define VO_METHOD_ENVELOPE 3
 
 typedef struct vo_ctx vo_ctx;
 typedef struct vo_volume vo_volume; /* a device-resident CSR volume */

@@ -21,7 +21,7 @@ LIB_PATH = os.path.join(PKG, "libvoroffset_gpu.so")
 VO_OK, VO_EINVAL, VO_ENOMEM, VO_ECUDA, VO_ERADIUS, VO_ERANGE, VO_ENODEV, VO_ETIMEOUT, VO_EINTERNAL = (
     0, -1, -2, -3, -4, -5, -6, -7, -8)
 OPS = {"dilation": 0, "erosion": 1, "opening": 2, "closing": 3}
-METHODS = {"separable": 0, "brute": 1, "fast": 2}
+METHODS = {"separable": 0, "brute": 1, "fast": 2, "envelope": 3}
 STATUS = {0: "VO_OK", -1: "VO_EINVAL", -2: "VO_ENOMEM", -3: "VO_ECUDA", -4: "VO_ERADIUS",
           -5: "VO_ERANGE", -6: "VO_ENODEV", -7: "VO_ETIMEOUT", -8: "VO_EINTERNAL"}
 

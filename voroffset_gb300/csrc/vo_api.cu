@@ -341,7 +341,8 @@ int vo_morph(vo_ctx *ctx, int op, int method, double radius, const vo_volume *in
   if (!ctx) return VO_EINVAL;
   if (!in || !out) return set_error(ctx, VO_EINVAL, "morph: NULL volume");
   if (op < VO_DILATION || op > VO_CLOSING) return set_error(ctx, VO_EINVAL, "morph: unknown op");
-  if (method != VO_METHOD_SEPARABLE && method != VO_METHOD_BRUTE && method != VO_METHOD_FAST)
+  if (method != VO_METHOD_SEPARABLE && method != VO_METHOD_BRUTE && method != VO_METHOD_FAST &&
+      method != VO_METHOD_ENVELOPE)
     return set_error(ctx, VO_EINVAL, "morph: unknown method");
   if (!(radius >= 0) || radius > 255) return set_error(ctx, VO_EINVAL, "morph: radius must be in [0, 255]");
   cudaSetDevice(ctx->device);

@@ -132,6 +132,11 @@ int get_tables(vo_ctx *ctx, double R, int kmax, const DeviceTables **out);
 // the total exceeds INT32_MAX.
 int scan_counts(vo_ctx *ctx, const int32_t *counts, int32_t *offs, int n, long long *total);
 
+// The separable scheme in its sweeping envelope form, FP64 (vo_env.cu).
+// Returns VO_OK, an error, or 1 when the volume exceeds the kernels' working
+// capacities and must take the painter form (VO_METHOD_SEPARABLE).
+int dilate_envelope(vo_ctx *ctx, double R, const vo_volume *in, vo_volume **out, vo_timings *tm);
+
 // Exact FP32-guarded separable dilation (vo_fast.cu).
 int dilate_fast(vo_ctx *ctx, double R, const vo_volume *in, vo_volume **out, vo_timings *tm);
 

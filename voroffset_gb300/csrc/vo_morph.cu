@@ -1007,6 +1007,17 @@ int dilate(vo_ctx *ctx, int method, double R, const vo_volume *in_user, vo_volum
   int nrc = normalize_inverted(ctx, in_user, &norm);
   if (nrc) return nrc;
   const vo_volume *in = norm ? norm : in_user;
+  if (method == VO_METHOD_ENVELOPE) {
+    nrc = dilate_envelope(ctx, R, in, out, tm);
+    if (nrc == 1) {  // beyond the sweeps' working capacities: the painter form has none
+      ctx->err.clear();
+      method = VO_METHOD_SEPARABLE;
+    } else {
+      if (norm) vo_volume_free(ctx, norm);
+      if (!nrc) (*out)->inverted = 0;
+      return nrc;
+    }
+  }
   if (method == VO_METHOD_FAST) {
     nrc = dilate_fast(ctx, R, in, out, tm);
     if (norm) vo_volume_free(ctx, norm);
