@@ -56,6 +56,7 @@ def parse():
                     help="batched: a captured batch plan with the learned sizer (the headline)")
     ap.add_argument("--no-sizer", action="store_true", help="batched plan without the learned sizer")
     ap.add_argument("--no-arms", action="store_true", help="skip the plain / single-volume comparison arms")
+    ap.add_argument("--no-learned-arm", action="store_true", help="skip the 4096^2 learned-sizing arm")
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--radius", type=float, default=RADIUS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -359,6 +360,49 @@ def batch_main(args, rank, world, local):
     return 0
 
 
+def learned_sizing_arm(ctx, sizer, rank, world, timed):
+    """The learned-sizing configuration: dilation r=16 of the 4096^2 volume of 20000 cylinders (radius
+    1.5-3, ~20 segments per column). One step each through a batch plan sized by the learned sizer, a
+    batch plan with fixed-capacity slots, and the single-volume FP32 method; a plan's step is a graph
+    replay (plus the re-run of a volume whose slots overflowed) and the conversion to CSR."""
+    import voroffset_gb300 as V
+    grid, offs, z = V.workload("cyl4096", seed=1 + rank)
+    v = ctx.upload(grid, offs, z)
+    ncols = grid.ncols
+    del offs, z
+    out = {"workload": "cyl4096 dilation r=16", "grid": [grid.nx, grid.ny]}
+    for name, sz in (("learned", sizer), ("fixed_capacity", None)):
+        if name == "learned" and sz is None:
+            continue
+        ctx.set_sizer(sz)
+        plan = ctx.batch([v], ["dilation"], [16.0], "fast")
+        st0 = plan.stats()
+
+        def step():
+            plan.run()
+            for o in plan.outputs():
+                o.free()
+
+        ms = timed(step, 1, 1)
+        st = plan.stats()
+        out[name] = {"value": job_rate(world, ncols, ms / 1e3), "unit": "Mcolumns/s", "ms_per_step": ms,
+                     "slot_bytes": st0["slot_bytes"], "volumes_rerun": st["reruns"], "plan_ms": st0["plan_ms"]}
+        plan.free()
+    ctx.set_sizer(sizer)
+
+    def single():
+        o, _ = ctx.morph(v, "dilation", 16.0, "fast")
+        o.free()
+
+    ms = timed(single, 1, 1)
+    out["single_volume"] = {"value": job_rate(world, ncols, ms / 1e3), "unit": "Mcolumns/s", "ms_per_step": ms}
+    if "learned" in out:
+        out["learned_vs_fixed"] = out["learned"]["value"] / out["fixed_capacity"]["value"]
+        out["learned_vs_single"] = out["learned"]["value"] / out["single_volume"]["value"]
+    v.free()
+    return out
+
+
 def sync_helpers(world: int, cuda: bool = True):
     """barrier(): device sync, then a barrier over the ranks; maxreduce(x): the
     largest x over the ranks (the job's time is its slowest rank's)."""
@@ -491,8 +535,9 @@ def main():
     if args.method == "batched" and not args.no_arms:
         # the plain method is the separable scheme's sweeping envelope form in FP64; the painter form
         # (per-column pass-1 pieces, then their union) is the other FP64 arm
-        for name, method, k in (("plain_envelope_fp64", "envelope", args.steps),
-                                ("painter_separable_fp64", "separable", max(1, args.steps // 2)),
+        # (the FP64 arms take seconds per step: two timed steps each keep the run within minutes)
+        for name, method, k in (("plain_envelope_fp64", "envelope", min(2, args.steps)),
+                                ("painter_separable_fp64", "separable", min(2, args.steps)),
                                 ("fast_single_volume", "fast", args.steps)):
             ms = timed(single_step(method), k, 1, after_warmup=lambda: acc.update(pass1_ms=0.0, pass2_ms=0.0))
             arms[name] = {"value": world * ncols * k / (ms / 1e3) / 1e6, "unit": "Mcolumns/s",
@@ -502,6 +547,8 @@ def main():
                 arms[name]["pass2_ms"] = acc.get("pass2_ms", 0.0) / k
         arms["batched_vs_plain"] = value / arms["plain_envelope_fp64"]["value"]
         arms["batched_vs_painter"] = value / arms["painter_separable_fp64"]["value"]
+        if not args.no_learned_arm:
+            arms["learned_sizing_cyl4096"] = learned_sizing_arm(ctx, sizer, rank, world, timed)
 
     # ---------------- end-to-end arm (pinned host buffers through the C ABI)
     pin_offs = torch.empty(offs.size, dtype=torch.int32, pin_memory=True).numpy()

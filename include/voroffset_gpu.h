@@ -179,6 +179,11 @@ int vo_dexelize(vo_ctx *ctx, const double *verts, int nv, const int32_t *tris, i
  * is never used; the CSR pairs here have no place for it and drop it. */
 int vo_dexelize_odd_columns(vo_ctx *ctx, int64_t *count);
 
+/* Segment count and enclosed volume of a volume, reduced on the device
+ * (CompressedVolume::numSegments and get_volume, CompressedVolume.cpp:61-83;
+ * volume in world units: spacing^3 times the summed segment lengths). */
+int vo_volume_measure(vo_ctx *ctx, const vo_volume *v, int64_t *num_segments, double *volume);
+
 /* Xor volume of two volumes on the same grid (Voronoi.cpp:91-111,
  * calculateXor's return value), computed on the device. */
 int vo_xor_volume(vo_ctx *ctx, const vo_volume *a, const vo_volume *b, double *volume);
@@ -202,6 +207,21 @@ int vo_xor_volume(vo_ctx *ctx, const vo_volume *a, const vo_volume *b, double *v
  * or threads) race and must be serialised by the caller. */
 int vo_xor_volume_noalloc(const vo_grid *grid, const int32_t *offs_a, const double *z_a,
                           const int32_t *offs_b, const double *z_b, void *stream, double *volume);
+
+/* ---- 2D images (src/vor2d CompressedImage: dilate / erode / open / close,
+ * CompressedImage.cpp:608-647) ----
+ * An image is `height` rows of `width` pixels (1 <= width <= 50000); row i is a
+ * sorted list of half-open pixel spans given as events [a0, b0, a1, b1, ...],
+ * strictly increasing within [0, width], in CSR form: row_offs[height + 1]
+ * counts events (the rows of CompressedImage, CompressedImage.h:32-41, and its
+ * save/load layout). op: VO_DILATION, VO_EROSION, VO_OPENING, VO_CLOSING with
+ * the reference's semantics (lattice disc of radius r, dy = floor(sqrt(r*r -
+ * t*t)); erosion treats everything outside the image as empty). The result is
+ * written to out_row_offs[height + 1] and out_events (capacity out_capacity
+ * events); when that is too small, VO_ERANGE is returned with the required
+ * count in out_row_offs[height]. radius in pixels, at most 1e6. */
+int vo_image_morph(vo_ctx *ctx, int op, double radius, int width, int height, const int32_t *row_offs,
+                   const int32_t *events, int32_t *out_row_offs, int32_t *out_events, int64_t out_capacity);
 
 /* ---- learned sizing for vo_morph_batched (no reference counterpart) ----
  * A small MLP (16 tile features -> 64 -> 64 -> 3 outputs, ReLU, BF16 weights

@@ -24,6 +24,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libvo_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libvor3d_ref.so")
+REF2D_SO = os.path.join(HERE, "_ref", "libvor2d_ref.so")
 # the package's input generator built from the same source (make oracle), so that the CPU baseline
 # makes its inputs without loading a product library
 SYNTH_SO = os.path.join(HERE, "_build", "libvo_synth.so")
@@ -97,6 +98,9 @@ def lib():
         L.vo_or_get_volume.restype = C.c_double
         L.vo_or_dilate_columns.argtypes = [G, V, C.c_double, C.POINTER(C.c_int32), C.c_int, C.c_int, V]
         L.vo_or_morph_columns.argtypes = [C.c_int, G, V, C.c_double, C.POINTER(C.c_int32), C.c_int, C.c_int, V]
+        L.vo_or_image_morph.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                        C.c_double, C.POINTER(C.POINTER(C.c_int32)),
+                                        C.POINTER(C.POINTER(C.c_int32))]
         L.vo_or_pass1_pieces.argtypes = [G, V, C.c_double, C.c_int]
         L.vo_or_pass1_pieces.restype = C.c_int64
         L.vo_or_dexelize.argtypes = [C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_int32), C.c_int,
@@ -266,6 +270,52 @@ def ref_morph(grid: Grid, offs, z, radius: float, op: str = "dilation", method: 
     L.ref_free(C.cast(po, C.c_void_p))
     L.ref_free(C.cast(pz, C.c_void_p))
     return o, zo, tms.value, t1.value, t2.value
+
+
+IMAGE_OPS = {"dilate": 0, "erode": 1, "open": 2, "close": 3}
+
+
+def _take_i32(p_offs, p_ev, height, free):
+    offs = np.ctypeslib.as_array(p_offs, shape=(height + 1,)).copy()
+    n = int(offs[-1])
+    ev = np.ctypeslib.as_array(p_ev, shape=(max(n, 1),))[:n].copy()
+    free(C.cast(p_offs, C.c_void_p))
+    free(C.cast(p_ev, C.c_void_p))
+    return offs, ev
+
+
+def image_morph(width: int, height: int, offs, events, radius: float, op: str = "dilate"):
+    """2D image morphology (src/vor2d CompressedImage), restated: returns (offs, events)."""
+    offs = np.ascontiguousarray(offs, dtype=np.int32)
+    ev = np.ascontiguousarray(events, dtype=np.int32)
+    if ev.size == 0:
+        ev = np.zeros(1, np.int32)
+    po, pe = C.POINTER(C.c_int32)(), C.POINTER(C.c_int32)()
+    rc = lib().vo_or_image_morph(IMAGE_OPS[op], int(width), int(height), offs.ctypes.data_as(C.POINTER(C.c_int32)),
+                                 ev.ctypes.data_as(C.POINTER(C.c_int32)), float(radius), C.byref(po), C.byref(pe))
+    _rc(rc, "vo_or_image_morph")
+    return _take_i32(po, pe, height, lib().vo_or_free)
+
+
+def ref2d_available() -> bool:
+    return os.path.exists(REF2D_SO)
+
+
+def ref_image_morph(width: int, height: int, offs, events, radius: float, op: str = "dilate"):
+    """The reference's own CompressedImage (oracle/_ref/libvor2d_ref.so): returns (offs, events)."""
+    L = C.CDLL(REF2D_SO)
+    L.ref2d_morph.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_double,
+                              C.POINTER(C.POINTER(C.c_int32)), C.POINTER(C.POINTER(C.c_int32))]
+    L.ref2d_free.argtypes = [C.c_void_p]
+    offs = np.ascontiguousarray(offs, dtype=np.int32)
+    ev = np.ascontiguousarray(events, dtype=np.int32)
+    if ev.size == 0:
+        ev = np.zeros(1, np.int32)
+    po, pe = C.POINTER(C.c_int32)(), C.POINTER(C.c_int32)()
+    rc = L.ref2d_morph(IMAGE_OPS[op], int(width), int(height), offs.ctypes.data_as(C.POINTER(C.c_int32)),
+                       ev.ctypes.data_as(C.POINTER(C.c_int32)), float(radius), C.byref(po), C.byref(pe))
+    _rc(rc, "ref2d_morph")
+    return _take_i32(po, pe, height, L.ref2d_free)
 
 
 def compare(a, b, tol: float = 1e-9):

@@ -1033,6 +1033,143 @@ int vo_or_morph_columns(int op, const vo_or_grid *g, const vo_or_csr *in, double
   return rc;
 }
 
+/* --------------------------------------------------------------- 2D images
+ *
+ * The reference's 2D library (src/vor2d): an image of `height` rows, each a
+ * sorted list of half-open pixel spans as events [a0, b0, a1, b1, ...]
+ * (CompressedImage.h:32-41). Restated as lattice unions:
+ *
+ * dilate (CompressedImage.cpp:608-616, Voronoi.cpp:749-759): row i is the union
+ *   over rows i0 with t = |i - i0| <= floor(r) of the spans [a, b) of row i0
+ *   widened to [max(a - dy, 0), min(b + dy, width)), dy = floor(sqrt(r*r - t*t));
+ *   touching spans merge (appendSegment, MorphologyOperators.cpp:10-29).
+ * erode (CompressedImage.cpp:620-630, Voronoi.h:126-150): the complement of the
+ *   same dilation applied to the complement spans of every row with one
+ *   border pixel on each side ([-1, a0 - 1], [b0, a1 - 1], ..., [b_last, width],
+ *   inclusive) and a full extra row before the first and after the last row.
+ * open / close: erode then dilate / dilate then erode (CompressedImage.cpp:634-647). */
+
+static int32_t img_dy(double r, int t) { return (int32_t)floor(sqrt(r * r - (double)((long long)t * t))); }
+
+/* Marks the union of [lo, hi) ranges in a difference array over [0, w]. */
+static void img_add(int32_t *diff, int w, int64_t lo, int64_t hi) {
+  if (lo < 0) lo = 0;
+  if (hi > w) hi = w;
+  if (lo >= hi) return;
+  diff[lo] += 1;
+  diff[hi] -= 1;
+}
+
+/* Covered pixels of row i under the dilation (erode = 0) or the dilation of the
+ * bordered complement (erode = 1); returns their spans as events. */
+static int img_row(int w, int h, const int32_t *offs, const int32_t *ev, double r, int erode, int i,
+                   int32_t *diff, int32_t *out) {
+  const int D = (int)floor(r);
+  memset(diff, 0, sizeof(int32_t) * ((size_t)w + 1));
+  for (int i0 = (i - D > -1 ? i - D : -1); i0 <= (i + D < h ? i + D : h); ++i0) {
+    const int t = i0 < i ? i - i0 : i0 - i;
+    if (erode && (i0 == -1 || i0 == h)) {
+      img_add(diff, w, 0, w);  /* the extra full row */
+      continue;
+    }
+    if (i0 < 0 || i0 >= h) continue;
+    const int32_t dy = img_dy(r, t);
+    const int32_t *e = ev + offs[i0];
+    const int n = offs[i0 + 1] - offs[i0];
+    if (!erode) {
+      for (int k = 0; k + 1 < n; k += 2) img_add(diff, w, (int64_t)e[k] - dy, (int64_t)e[k + 1] + dy);
+    } else {
+      int64_t y1 = -1;
+      for (int k = 0; k + 1 < n; k += 2) {
+        img_add(diff, w, y1 - dy, (int64_t)e[k] - 1 + dy + 1);
+        y1 = e[k + 1];
+      }
+      img_add(diff, w, y1 - dy, (int64_t)w + dy + 1);
+    }
+  }
+  int k = 0, c = 0, prev = 0;
+  for (int p = 0; p <= w; ++p) {
+    c += diff[p];
+    const int cov = p < w && c > 0;
+    if (cov != prev) out[k++] = p;
+    prev = cov;
+  }
+  return k;
+}
+
+static int img_apply(int op1, int w, int h, const int32_t *offs, const int32_t *ev, double r, int32_t **oo,
+                     int32_t **oe) {
+  int32_t *diff = (int32_t *)malloc(sizeof(int32_t) * ((size_t)w + 2));
+  int32_t *row = (int32_t *)malloc(sizeof(int32_t) * ((size_t)w + 2));
+  int32_t *ro = (int32_t *)malloc(sizeof(int32_t) * ((size_t)h + 1));
+  int64_t cap = 16, used = 0;
+  int32_t *re = (int32_t *)malloc(sizeof(int32_t) * cap);
+  if (!diff || !row || !ro || !re) {
+    free(diff); free(row); free(ro); free(re);
+    return VO_OR_ENOMEM;
+  }
+  ro[0] = 0;
+  for (int i = 0; i < h; ++i) {
+    int n = img_row(w, h, offs, ev, r, op1, i, diff, row);
+    if (op1) {  /* erosion: complement of the covered spans within [0, w) (negate, CompressedImage.cpp:366-397) */
+      int m = 0;
+      int32_t *neg = diff; /* reuse as scratch */
+      if (n == 0) {
+        neg[m++] = 0;
+        neg[m++] = w;
+      } else {
+        if (row[0] != 0) neg[m++] = 0;
+        for (int k = (row[0] == 0 ? 1 : 0); k < n; ++k) neg[m++] = row[k];
+        if (row[n - 1] == w) --m;
+        else neg[m++] = w;
+      }
+      memcpy(row, neg, sizeof(int32_t) * m);
+      n = m;
+    }
+    if (used + n > cap) {
+      while (used + n > cap) cap *= 2;
+      int32_t *t = (int32_t *)realloc(re, sizeof(int32_t) * cap);
+      if (!t) {
+        free(diff); free(row); free(ro); free(re);
+        return VO_OR_ENOMEM;
+      }
+      re = t;
+    }
+    memcpy(re + used, row, sizeof(int32_t) * n);
+    used += n;
+    ro[i + 1] = (int32_t)used;
+  }
+  free(diff);
+  free(row);
+  *oo = ro;
+  *oe = re;
+  return VO_OR_OK;
+}
+
+int vo_or_image_morph(int op, int width, int height, const int32_t *offs, const int32_t *events, double radius,
+                      int32_t **out_offs, int32_t **out_events) {
+  if (width < 0 || height < 0 || !offs || !out_offs || !out_events || !(radius >= 0) || op < 0 || op > 3)
+    return VO_OR_EINVAL;
+  int32_t *o1 = NULL, *e1 = NULL;
+  int rc;
+  switch (op) {
+    case 0:
+    case 1:
+      return img_apply(op, width, height, offs, events, radius, out_offs, out_events);
+    case 2:
+      rc = img_apply(1, width, height, offs, events, radius, &o1, &e1);
+      if (!rc) rc = img_apply(0, width, height, o1, e1, radius, out_offs, out_events);
+      break;
+    default:
+      rc = img_apply(0, width, height, offs, events, radius, &o1, &e1);
+      if (!rc) rc = img_apply(1, width, height, o1, e1, radius, out_offs, out_events);
+      break;
+  }
+  free(o1);
+  free(e1);
+  return rc;
+}
+
 /* --------------------------------------------------------------- xor */
 
 static int union_segs(const double *a, int na2, const double *b, int nb2, double *out) {

@@ -53,6 +53,11 @@ int vo_or_dilate_brute(const vo_or_grid *g, const vo_or_csr *in, double radius, 
 /* op: 0 dilation, 1 erosion, 2 opening, 3 closing; method: 0 separable, 1 brute. */
 int vo_or_morph(int method, int op, const vo_or_grid *g, const vo_or_csr *in, double radius,
                 int nthreads, vo_or_csr *out);
+/* 2D images (src/vor2d CompressedImage): op 0 dilate, 1 erode, 2 open, 3 close of
+ * an image of `height` rows of `width` pixels, rows as half-open span events in
+ * CSR form (offs[height + 1] counts events). */
+int vo_or_image_morph(int op, int width, int height, const int32_t *offs, const int32_t *events, double radius,
+                      int32_t **out_offs, int32_t **out_events);
 /* Xor volume (Voronoi.cpp:91-111). */
 double vo_or_xor_volume(const vo_or_grid *g, const vo_or_csr *a, const vo_or_csr *b);
 double vo_or_get_volume(const vo_or_grid *g, const vo_or_csr *a);

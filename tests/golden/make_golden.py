@@ -2,7 +2,9 @@
 
 Runs the reference's own vor3d sources (compiled unmodified into
 oracle/_ref/libvor3d_ref.so by ``make -C oracle ref``) on small seeded
-inputs and stores inputs and outputs as .npz. The reference source tree is
+inputs and stores inputs and outputs as .npz; likewise its vor2d
+CompressedImage (oracle/_ref/libvor2d_ref.so) on seeded images, into
+tests/golden/2d/. The reference source tree is
 needed to build that library, so this script runs in the development
 container only; the fixtures it writes travel with the repository and pin the
 oracle restatement wherever the reference itself is absent.
@@ -34,6 +36,15 @@ CASES = [
 ]
 OPS = ["dilation", "erosion", "opening", "closing"]
 
+# 2D images: (name, width, height, blob count, seed, pixel noise, radius)
+IMAGE_CASES = [
+    ("blobs64x48_r4", 64, 48, 14, 21, 0.0, 4.0),
+    ("blobs97x61_r6p5", 97, 61, 20, 22, 0.0, 6.5),
+    ("noisy40x33_r2p5", 40, 33, 6, 23, 0.15, 2.5),
+    ("thin1x50_r3", 1, 50, 3, 24, 0.3, 3.0),
+]
+IMAGE_OPS = {"dilation": "dilate", "erosion": "erode", "opening": "open", "closing": "close"}
+
 
 def main():
     O.build(ref=True)
@@ -46,6 +57,16 @@ def main():
     og, offs, z = O.dexelize(verts, tris, num_dexels=40, padding=4)
     grid = V.Grid(og.nx, og.ny, og.origin, og.extent, og.spacing, og.padding)
     _write("torus40_p4_r3", grid, offs, z, 3.0, verts=verts, tris=tris)
+    sys.path.insert(0, os.path.dirname(HERE))
+    from imageutil import blobs
+    for name, w, h, n, seed, noise, r in IMAGE_CASES:
+        offs, ev = blobs(w, h, n, seed, noise=noise)
+        out = {"width": w, "height": h, "radius": r, "offs": offs, "events": ev}
+        for op, rop in IMAGE_OPS.items():
+            out[f"{op}_offs"], out[f"{op}_events"] = O.ref_image_morph(w, h, offs, ev, r, rop)
+        path = os.path.join(HERE, "2d", f"{name}.npz")
+        np.savez_compressed(path, **out)
+        print(path, os.path.getsize(path), "bytes")
 
 
 def _write(name, grid, offs, z, r, **extra):

@@ -196,6 +196,21 @@ def test_gpu_xor_volume(ctx, vo, oracle):
     assert got == pytest.approx(want, rel=1e-12)
 
 
+def test_gpu_measure_matches_oracle(ctx, vo, oracle):
+    """numSegments / get_volume (CompressedVolume.cpp:61-83) on the device; the volume is a sum in a
+    different order from the reference's sequential one, so it agrees to rounding."""
+    grid, offs, z = vo.synth_volume(vo.SynthSpec(80, ny=70, n_spheres=40, s_rmin=2, s_rmax=15, n_cyl=6, seed=44))
+    g2 = vo.Grid(grid.nx, grid.ny, grid.origin, grid.extent, 0.25, 0)  # spacing enters as spacing^3
+    for g in (grid, g2):
+        v = ctx.upload(g, offs, z)
+        n, vol = ctx.measure(v)
+        assert n == int(offs[-1])
+        assert vol == pytest.approx(oracle.get_volume(ogrid(oracle, g), offs, z), rel=1e-12)
+        v.free()
+    empty = ctx.upload(grid, np.zeros(grid.ncols + 1, np.int32), np.zeros(0))
+    assert ctx.measure(empty) == (0, 0.0)
+
+
 def test_gpu_dexelize_matches_oracle(ctx, vo, oracle):
     verts, tris = vo.synth_torus(256, 64, 0.30, 0.10, 0.01, seed=1)
     og, offs, z = oracle.dexelize(verts, tris, num_dexels=128, padding=10)

@@ -113,6 +113,9 @@ SIGNATURES = {
                               C.POINTER(C.c_double), C.c_int, C.c_int, C.POINTER(_P)]),
     "vo_dexelize_odd_columns": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "vo_xor_volume": (C.c_int, [_P, _P, _P, C.POINTER(C.c_double)]),
+    "vo_volume_measure": (C.c_int, [_P, _P, C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
+    "vo_image_morph": (C.c_int, [_P, C.c_int, C.c_double, C.c_int, C.c_int, C.POINTER(C.c_int32),
+                                 C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_int64]),
     "vo_xor_volume_noalloc": (C.c_int, [C.POINTER(_Grid), _P, _P, _P, _P, _P, C.POINTER(C.c_double)]),
     "vo_batch_create": (C.c_int, [_P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_int,
                                   C.POINTER(_P), C.POINTER(_P)]),
@@ -336,6 +339,30 @@ class Context:
         n = C.c_int64()
         self._check(lib().vo_dexelize_odd_columns(self.handle, C.byref(n)), "vo_dexelize_odd_columns")
         return int(n.value)
+
+    def image_morph(self, width: int, height: int, row_offs, events, radius: float, op: str = "dilation"):
+        """2D image morphology (CompressedImage): returns (row_offs, events) of the result."""
+        ro = np.ascontiguousarray(row_offs, dtype=np.int32)
+        ev = np.ascontiguousarray(events, dtype=np.int32)
+        if ev.size == 0:
+            ev = np.zeros(1, np.int32)
+        out_o = np.zeros(height + 1, np.int32)
+        cap = max(16, 2 * int(ro[-1]) + 2 * height)
+        while True:
+            out_e = np.zeros(cap, np.int32)
+            rc = lib().vo_image_morph(self.handle, OPS[op], float(radius), int(width), int(height), _i32p(ro),
+                                      _i32p(ev), _i32p(out_o), _i32p(out_e), cap)
+            if rc == VO_ERANGE and int(out_o[-1]) > cap:
+                cap = int(out_o[-1])
+                continue
+            self._check(rc, "vo_image_morph")
+            return out_o, out_e[:int(out_o[-1])].copy()
+
+    def measure(self, v: Volume):
+        """(numSegments, get_volume) of a volume, reduced on the device."""
+        n, vol = C.c_int64(), C.c_double()
+        self._check(lib().vo_volume_measure(self.handle, v.handle, C.byref(n), C.byref(vol)), "vo_volume_measure")
+        return int(n.value), float(vol.value)
 
     def xor_volume(self, a: Volume, b: Volume) -> float:
         r = C.c_double()

@@ -8,6 +8,7 @@
 // touching pieces), and runs shorter than 1e-10 are dropped like removepoint.
 // Column lengths are summed per block and the block partials are added in a
 // fixed order, so the result is deterministic.
+#include <algorithm>
 #include <mutex>
 
 #include "vo_internal.cuh"
@@ -78,10 +79,70 @@ __global__ void k_sum(const double *partial, int n, double *out) {
   if (threadIdx.x == 0) *out = s[0];
 }
 
+// Segment count and volume (CompressedVolume::numSegments / get_volume,
+// CompressedVolume.cpp:61-83): per segment h^3 * (z2 - z1), as the reference
+// adds it, summed per block of columns, then the block partials in a fixed
+// order (deterministic; the reference's sequential sum rounds differently, by
+// relative amounts of order 1e-15 times the segment count).
+__global__ void k_measure(int ncols, const int32_t *__restrict__ offs, const double2 *__restrict__ z, double h3,
+                          double *__restrict__ partial, unsigned long long *__restrict__ nseg) {
+  __shared__ double s[kThreads];
+  const int c = blockIdx.x * kThreads + threadIdx.x;
+  double v = 0;
+  unsigned long long n = 0;
+  if (c < ncols) {
+    for (int k = offs[c]; k < offs[c + 1]; ++k) v += h3 * (z[k].y - z[k].x);
+    n = (unsigned long long)(offs[c + 1] - offs[c]);
+  }
+  for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
+  if ((threadIdx.x & 31) == 0 && n) atomicAdd(nseg, n);
+  s[threadIdx.x] = v;
+  __syncthreads();
+  for (int o = kThreads / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) s[threadIdx.x] += s[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = s[0];
+}
+
 }  // namespace
 }  // namespace vo
 
 using namespace vo;
+
+extern "C" int vo_volume_measure(vo_ctx *ctx, const vo_volume *v, int64_t *num_segments, double *volume) {
+  if (!ctx) return VO_EINVAL;
+  if (!v || !num_segments || !volume) return set_error(ctx, VO_EINVAL, "measure: NULL argument");
+  cudaSetDevice(ctx->device);
+  ctx->err.clear();
+  const int ncols = v->grid.nx * v->grid.ny;
+  const int nblk = std::max(1, (ncols + kThreads - 1) / kThreads);
+  double *partial = nullptr, *d_out = nullptr;
+  int rc = dalloc(ctx, &partial, (size_t)nblk);
+  if (!rc) rc = dalloc(ctx, &d_out, 1);
+  if (rc) {
+    dfree(ctx, partial);
+    return rc;
+  }
+  unsigned long long *d_n = reinterpret_cast<unsigned long long *>(ctx->d_total);
+  cudaMemsetAsync(d_n, 0, sizeof(unsigned long long), ctx->stream);
+  cudaMemsetAsync(partial, 0, sizeof(double) * nblk, ctx->stream);
+  const double h = v->grid.spacing;
+  if (ncols > 0)
+    k_measure<<<nblk, kThreads, 0, ctx->stream>>>(ncols, v->offs, v->z, h * h * h, partial, d_n);
+  k_sum<<<1, kThreads, 0, ctx->stream>>>(partial, nblk, d_out);
+  double hv = 0;
+  unsigned long long hn = 0;
+  cudaMemcpyAsync(&hv, d_out, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+  cudaMemcpyAsync(&hn, d_n, sizeof hn, cudaMemcpyDeviceToHost, ctx->stream);
+  dfree(ctx, partial);
+  dfree(ctx, d_out);
+  VO_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  VO_CK(ctx, cudaGetLastError());
+  *num_segments = (int64_t)hn;
+  *volume = hv;
+  return VO_OK;
+}
 
 extern "C" int vo_xor_volume(vo_ctx *ctx, const vo_volume *a, const vo_volume *b, double *volume) {
   if (!ctx) return VO_EINVAL;
