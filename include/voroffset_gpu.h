@@ -223,6 +223,15 @@ int vo_xor_volume_noalloc(const vo_grid *grid, const int32_t *offs_a, const doub
 int vo_image_morph(vo_ctx *ctx, int op, double radius, int width, int height, const int32_t *row_offs,
                    const int32_t *events, int32_t *out_row_offs, int32_t *out_events, int64_t out_capacity);
 
+/* The FP64 twin (src/vor2d DoubleCompressedImage, DoubleCompressedImage.cpp:680-720):
+ * rows of closed spans with FP64 events sorted within [0, width]. As in the
+ * reference, dilation scales the radius by the row count (R = radius * height,
+ * at most 255 after scaling) and erosion uses it as given; erosion treats
+ * everything outside the image as empty. Output and VO_ERANGE as for
+ * vo_image_morph. */
+int vo_image_morph_f64(vo_ctx *ctx, int op, double radius, int width, int height, const int32_t *row_offs,
+                       const double *events, int32_t *out_row_offs, double *out_events, int64_t out_capacity);
+
 /* ---- learned sizing for vo_morph_batched (no reference counterpart) ----
  * A small MLP (16 tile features -> 64 -> 64 -> 3 outputs, ReLU, BF16 weights
  * with FP32 accumulation) predicts per 32 x 32 tile of output columns

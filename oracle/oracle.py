@@ -101,6 +101,9 @@ def lib():
         L.vo_or_image_morph.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                         C.c_double, C.POINTER(C.POINTER(C.c_int32)),
                                         C.POINTER(C.POINTER(C.c_int32))]
+        L.vo_or_image_morph_f64.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int32),
+                                            C.POINTER(C.c_double), C.c_double, C.POINTER(C.POINTER(C.c_int32)),
+                                            C.POINTER(C.POINTER(C.c_double))]
         L.vo_or_pass1_pieces.argtypes = [G, V, C.c_double, C.c_int]
         L.vo_or_pass1_pieces.restype = C.c_int64
         L.vo_or_dexelize.argtypes = [C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_int32), C.c_int,
@@ -295,6 +298,45 @@ def image_morph(width: int, height: int, offs, events, radius: float, op: str = 
                                  ev.ctypes.data_as(C.POINTER(C.c_int32)), float(radius), C.byref(po), C.byref(pe))
     _rc(rc, "vo_or_image_morph")
     return _take_i32(po, pe, height, lib().vo_or_free)
+
+
+def _take_f64(p_offs, p_ev, height, free):
+    offs = np.ctypeslib.as_array(p_offs, shape=(height + 1,)).copy()
+    n = int(offs[-1])
+    ev = np.ctypeslib.as_array(p_ev, shape=(max(n, 1),))[:n].copy()
+    free(C.cast(p_offs, C.c_void_p))
+    free(C.cast(p_ev, C.c_void_p))
+    return offs, ev
+
+
+def image_morph_f64(width: int, height: int, offs, events, radius: float, op: str = "dilate"):
+    """The FP64 twin (DoubleCompressedImage), restated: returns (offs, events)."""
+    offs = np.ascontiguousarray(offs, dtype=np.int32)
+    ev = np.ascontiguousarray(events, dtype=np.float64)
+    if ev.size == 0:
+        ev = np.zeros(1)
+    po, pe = C.POINTER(C.c_int32)(), C.POINTER(C.c_double)()
+    rc = lib().vo_or_image_morph_f64(IMAGE_OPS[op], int(width), int(height), offs.ctypes.data_as(C.POINTER(C.c_int32)),
+                                     ev.ctypes.data_as(C.POINTER(C.c_double)), float(radius), C.byref(po), C.byref(pe))
+    _rc(rc, "vo_or_image_morph_f64")
+    return _take_f64(po, pe, height, lib().vo_or_free)
+
+
+def ref_image_morph_f64(width: int, height: int, offs, events, radius: float, op: str = "dilate"):
+    """The reference's own DoubleCompressedImage (oracle/_ref/libvor2d_ref.so)."""
+    L = C.CDLL(REF2D_SO)
+    L.ref2d_morph_f64.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int32), C.POINTER(C.c_double),
+                                  C.c_double, C.POINTER(C.POINTER(C.c_int32)), C.POINTER(C.POINTER(C.c_double))]
+    L.ref2d_free.argtypes = [C.c_void_p]
+    offs = np.ascontiguousarray(offs, dtype=np.int32)
+    ev = np.ascontiguousarray(events, dtype=np.float64)
+    if ev.size == 0:
+        ev = np.zeros(1)
+    po, pe = C.POINTER(C.c_int32)(), C.POINTER(C.c_double)()
+    rc = L.ref2d_morph_f64(IMAGE_OPS[op], int(width), int(height), offs.ctypes.data_as(C.POINTER(C.c_int32)),
+                           ev.ctypes.data_as(C.POINTER(C.c_double)), float(radius), C.byref(po), C.byref(pe))
+    _rc(rc, "ref2d_morph_f64")
+    return _take_f64(po, pe, height, L.ref2d_free)
 
 
 def ref2d_available() -> bool:

@@ -65,3 +65,46 @@ extern "C" int ref2d_morph(int op, int width, int height, const int32_t *offs, c
 }
 
 extern "C" void ref2d_free(void *p) { std::free(p); }
+
+// The FP64 twin, DoubleCompressedImage (DoubleCompressedImage.cpp:680-720):
+// rows of closed spans with FP64 events; dilate scales its radius by the row
+// count, erode does not (as the reference does).
+#include "vor2d/DoubleCompressedImage.h"
+
+extern "C" int ref2d_morph_f64(int op, int width, int height, const int32_t *offs, const double *events,
+                               double radius, int32_t **out_offs, double **out_events) {
+  try {
+    std::ostringstream in;
+    in.precision(17);
+    in << width << ' ' << height << '\n';
+    for (int i = 0; i < height; ++i) {
+      in << (offs[i + 1] - offs[i]);
+      for (int k = offs[i]; k < offs[i + 1]; ++k) in << ' ' << events[k];
+      in << '\n';
+    }
+    std::istringstream is(in.str());
+    voroffset::DoubleCompressedImage img(is);
+    switch (op) {
+      case 0: img.dilate(radius); break;
+      case 1: img.erode(radius); break;
+      case 2: img.open(radius); break;
+      case 3: img.close(radius); break;
+      default: return -1;
+    }
+    std::vector<int32_t> o(1, 0);
+    std::vector<double> e;
+    for (int i = 0; i < img.height(); ++i) {
+      const auto &row = img.at(i);
+      e.insert(e.end(), row.begin(), row.end());
+      o.push_back((int32_t)e.size());
+    }
+    *out_offs = (int32_t *)std::malloc(sizeof(int32_t) * o.size());
+    *out_events = (double *)std::malloc(sizeof(double) * (e.size() + 1));
+    if (!*out_offs || !*out_events) return -3;
+    std::memcpy(*out_offs, o.data(), sizeof(int32_t) * o.size());
+    if (!e.empty()) std::memcpy(*out_events, e.data(), sizeof(double) * e.size());
+    return 0;
+  } catch (...) {
+    return -4;
+  }
+}

@@ -1170,6 +1170,129 @@ int vo_or_image_morph(int op, int width, int height, const int32_t *offs, const 
   return rc;
 }
 
+/* The FP64 twin (DoubleCompressedImage.cpp:680-720): rows of closed spans with
+ * FP64 events in [0, width].
+ * dilate: radius scaled by the row count, R = r * height; row i is the union
+ *   over rows i0 with |i - i0| <= floor(R) of [y1 - dy, y2 + dy], dy =
+ *   sqrt(R*R - t*t) (VoronoiMorphoF::getLine, DoubleVoronoi.cpp:713-726) — the
+ *   3D dilation of a one-row grid — clamped to [0, width], intervals wholly
+ *   outside dropped.
+ * erode: radius as given; the complement spans [-1, a0], [b0, a1], ...,
+ *   [b_last, width] of every row plus a full row [-1, width] before the first
+ *   and after the last (voronoiF_half_erode, DoubleVoronoi.h:124-148), dilated,
+ *   clamped the same way, then negate (DoubleCompressedImage.cpp:438-470). */
+
+static int img64_dilate_rows(int nrows, const int32_t *soffs, const double *z, double R, vo_or_csr *out) {
+  vo_or_grid g;
+  memset(&g, 0, sizeof g);
+  g.nx = nrows;
+  g.ny = 1;
+  g.spacing = 1.0;
+  vo_or_csr in = {(int32_t *)soffs, (double *)z};
+  return vo_or_dilate(&g, &in, R, 1, out, NULL, NULL);
+}
+
+/* Clamps row i (segments of rows[row0 + i]) to [0, w], optionally negates it, appends events. */
+static int64_t img64_clip_row(const vo_or_csr *v, int row, double w, int negate, double *dst) {
+  double tmp_lo, tmp_hi;
+  int64_t k = 0;
+  for (int s = v->offs[row]; s < v->offs[row + 1]; ++s) {
+    tmp_lo = v->z[2 * s];
+    tmp_hi = v->z[2 * s + 1];
+    if (tmp_hi < 0 || tmp_lo > w) continue;
+    dst[k++] = tmp_lo > 0 ? tmp_lo : 0;
+    dst[k++] = tmp_hi < w ? tmp_hi : w;
+  }
+  if (!negate) return k;
+  if (k == 0) {
+    dst[0] = 0;
+    dst[1] = w;
+    return 2;
+  }
+  /* first event: drop a leading 0, else prepend 0; last: drop a trailing w, else append w */
+  int64_t m = 0;
+  double *o = dst + k + 1;  /* scratch after the clipped events */
+  if (dst[0] != 0) o[m++] = 0;
+  for (int64_t q = (dst[0] == 0 ? 1 : 0); q < k; ++q) o[m++] = dst[q];
+  if (dst[k - 1] == w) --m;
+  else o[m++] = w;
+  memmove(dst, o, sizeof(double) * m);
+  return m;
+}
+
+static int img64_apply(int erode, int w, int h, const int32_t *offs, const double *ev, double r, int32_t **oo,
+                       double **oe) {
+  const int nr = erode ? h + 2 : h;
+  int32_t *so = (int32_t *)malloc(sizeof(int32_t) * ((size_t)nr + 1));
+  int64_t nval = erode ? (int64_t)offs[h] + 2 * (int64_t)h + 4 : (int64_t)offs[h];
+  double *sz = (double *)malloc(sizeof(double) * (size_t)(nval + 2));
+  if (!so || !sz) {
+    free(so); free(sz);
+    return VO_OR_ENOMEM;
+  }
+  so[0] = 0;
+  int64_t q = 0;
+  if (!erode) {
+    memcpy(sz, ev, sizeof(double) * (size_t)offs[h]);
+    for (int i = 0; i < h; ++i) so[i + 1] = offs[i + 1] / 2;
+  } else {
+    for (int rr = 0; rr < nr; ++rr) {
+      if (rr == 0 || rr == nr - 1) {
+        sz[q++] = -1;
+        sz[q++] = w;
+      } else {
+        const int i = rr - 1;
+        double y1 = -1;
+        for (int k = offs[i]; k + 1 < offs[i + 1]; k += 2) {
+          sz[q++] = y1;
+          sz[q++] = ev[k];
+          y1 = ev[k + 1];
+        }
+        sz[q++] = y1;
+        sz[q++] = w;
+      }
+      so[rr + 1] = (int32_t)(q / 2);
+    }
+  }
+  vo_or_csr dil = {0};
+  int rc = img64_dilate_rows(nr, so, sz, erode ? r : r * h, &dil);
+  free(so);
+  free(sz);
+  if (rc) return rc;
+  int32_t *ro = (int32_t *)malloc(sizeof(int32_t) * ((size_t)h + 1));
+  double *re = (double *)malloc(sizeof(double) * (size_t)(2 * (int64_t)dil.offs[nr] * 2 + 4 * (int64_t)h + 8));
+  if (!ro || !re) {
+    free(ro); free(re); free(dil.offs); free(dil.z);
+    return VO_OR_ENOMEM;
+  }
+  int64_t used = 0;
+  ro[0] = 0;
+  for (int i = 0; i < h; ++i) {
+    used += img64_clip_row(&dil, erode ? i + 1 : i, (double)w, erode, re + used);
+    ro[i + 1] = (int32_t)used;
+  }
+  free(dil.offs);
+  free(dil.z);
+  *oo = ro;
+  *oe = re;
+  return VO_OR_OK;
+}
+
+int vo_or_image_morph_f64(int op, int width, int height, const int32_t *offs, const double *events, double radius,
+                          int32_t **out_offs, double **out_events) {
+  if (width < 0 || height < 0 || !offs || !out_offs || !out_events || !(radius >= 0) || op < 0 || op > 3)
+    return VO_OR_EINVAL;
+  int32_t *o1 = NULL;
+  double *e1 = NULL;
+  int rc;
+  if (op == 0 || op == 1) return img64_apply(op, width, height, offs, events, radius, out_offs, out_events);
+  rc = img64_apply(op == 2 ? 1 : 0, width, height, offs, events, radius, &o1, &e1);
+  if (!rc) rc = img64_apply(op == 2 ? 0 : 1, width, height, o1, e1, radius, out_offs, out_events);
+  free(o1);
+  free(e1);
+  return rc;
+}
+
 /* --------------------------------------------------------------- xor */
 
 static int union_segs(const double *a, int na2, const double *b, int nb2, double *out) {

@@ -58,6 +58,10 @@ int vo_or_morph(int method, int op, const vo_or_grid *g, const vo_or_csr *in, do
  * CSR form (offs[height + 1] counts events). */
 int vo_or_image_morph(int op, int width, int height, const int32_t *offs, const int32_t *events, double radius,
                       int32_t **out_offs, int32_t **out_events);
+/* The FP64 twin (DoubleCompressedImage): rows of closed spans with FP64 events;
+ * dilate scales the radius by the row count, erode does not. */
+int vo_or_image_morph_f64(int op, int width, int height, const int32_t *offs, const double *events, double radius,
+                          int32_t **out_offs, double **out_events);
 /* Xor volume (Voronoi.cpp:91-111). */
 double vo_or_xor_volume(const vo_or_grid *g, const vo_or_csr *a, const vo_or_csr *b);
 double vo_or_get_volume(const vo_or_grid *g, const vo_or_csr *a);

@@ -44,6 +44,12 @@ IMAGE_CASES = [
     ("thin1x50_r3", 1, 50, 3, 24, 0.3, 3.0),
 ]
 IMAGE_OPS = {"dilation": "dilate", "erosion": "erode", "opening": "open", "closing": "close"}
+# FP64 twin (DoubleCompressedImage): (name, width, height, seed, spans per row, radius); dilation
+# scales the radius by the row count, erosion does not
+IMAGE64_CASES = [
+    ("f64_50x40_r0p05", 50, 40, 31, 3, 0.05),
+    ("f64_33x70_r1p5", 33, 70, 32, 4, 1.5),
+]
 
 
 def main():
@@ -64,6 +70,15 @@ def main():
         out = {"width": w, "height": h, "radius": r, "offs": offs, "events": ev}
         for op, rop in IMAGE_OPS.items():
             out[f"{op}_offs"], out[f"{op}_events"] = O.ref_image_morph(w, h, offs, ev, r, rop)
+        path = os.path.join(HERE, "2d", f"{name}.npz")
+        np.savez_compressed(path, **out)
+        print(path, os.path.getsize(path), "bytes")
+    from imageutil import random_f64
+    for name, w, h, seed, k, r in IMAGE64_CASES:
+        offs, ev = random_f64(w, h, seed, k)
+        out = {"width": w, "height": h, "radius": r, "offs": offs, "events": ev}
+        for op, rop in IMAGE_OPS.items():
+            out[f"{op}_offs"], out[f"{op}_events"] = O.ref_image_morph_f64(w, h, offs, ev, r, rop)
         path = os.path.join(HERE, "2d", f"{name}.npz")
         np.savez_compressed(path, **out)
         print(path, os.path.getsize(path), "bytes")

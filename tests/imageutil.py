@@ -45,3 +45,20 @@ def blobs(w, h, n, seed, rmax=12.0, noise=0.0):
     if noise > 0:
         m ^= rng.random((h, w)) < noise
     return from_mask(m)
+
+
+def random_f64(w, h, seed, max_spans=4):
+    """Rows of sorted FP64 events in [0, w] (closed spans, some zero-length and touching)."""
+    rng = np.random.default_rng(seed)
+    offs = [0]
+    ev = []
+    for _ in range(h):
+        k = int(rng.integers(0, max_spans + 1))
+        v = np.sort(rng.uniform(0, w, 2 * k))
+        if k and rng.random() < 0.2:
+            v[1] = v[0]  # a point span
+        if k > 1 and rng.random() < 0.2:
+            v[2] = v[1]  # touching spans
+        ev.extend(v.tolist())
+        offs.append(len(ev))
+    return np.array(offs, np.int32), np.array(ev, np.float64)

@@ -7,7 +7,10 @@ CompressedImage.cpp:608-647) dilated, eroded, opened and closed.
 * the GPU (vo_image_morph, through the C ABI) against the fixtures and the
   oracle, bit for bit (integer pixel spans), including one-pixel-wide and
   one-row images, empty and full rows, integer radii and radius 0, and its
-  argument checks."""
+  argument checks;
+* the FP64 twin (DoubleCompressedImage, DoubleCompressedImage.cpp:680-720) the
+  same way: oracle against fixtures written by the reference's own build and
+  against that build; vo_image_morph_f64 against both, bit for bit."""
 from __future__ import annotations
 
 import ctypes as C
@@ -18,9 +21,11 @@ import numpy as np
 import pytest
 
 from conftest import ROOT
-from imageutil import blobs, from_mask
+from imageutil import blobs, from_mask, random_f64
 
-GOLDEN2D = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "2d", "*.npz")))
+GOLDEN2D = sorted(p for p in glob.glob(os.path.join(ROOT, "tests", "golden", "2d", "*.npz"))
+                  if not os.path.basename(p).startswith("f64_"))
+GOLDEN2D_F64 = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "2d", "f64_*.npz")))
 OPS = {"dilation": "dilate", "erosion": "erode", "opening": "open", "closing": "close"}
 
 
@@ -106,3 +111,55 @@ def test_gpu_image_capacity_and_argument_checks(ctx, vo):
     assert rc == vo.VO_ERADIUS
     rc = vo.lib().vo_image_morph(ctx.handle, 9, 3.0, 50, 40, p(offs), p(ev), p(out_o), p(out_e), 2)
     assert rc == vo.VO_EINVAL
+
+
+@pytest.mark.parametrize("path", GOLDEN2D_F64, ids=lambda p: os.path.basename(p)[:-4])
+@pytest.mark.parametrize("op", list(OPS))
+def test_oracle_image_f64_matches_reference_fixture(oracle, path, op):
+    d = np.load(path)
+    got = oracle.image_morph_f64(int(d["width"]), int(d["height"]), d["offs"], d["events"], float(d["radius"]),
+                                 OPS[op])
+    assert np.array_equal(got[0], d[f"{op}_offs"]) and np.array_equal(got[1], d[f"{op}_events"])
+
+
+def test_oracle_image_f64_matches_reference_build(oracle):
+    if not oracle.ref2d_available():
+        pytest.skip("reference sources absent: pinned by the fixtures instead")
+    rng = np.random.default_rng(4)
+    for trial in range(40):
+        w, h = int(rng.integers(1, 60)), int(rng.integers(1, 60))
+        offs, ev = random_f64(w, h, int(rng.integers(1, 1 << 30)), int(rng.integers(0, 6)))
+        for op, r in (("dilate", float(rng.choice([0.0, 0.02, 0.1]))), ("erode", float(rng.choice([0.0, 1.0, 3.5]))),
+                      ("open", 0.05), ("close", 0.04)):
+            a = oracle.image_morph_f64(w, h, offs, ev, r, op)
+            b = oracle.ref_image_morph_f64(w, h, offs, ev, r, op)
+            assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]), (trial, w, h, r, op)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("path", GOLDEN2D_F64, ids=lambda p: os.path.basename(p)[:-4])
+def test_gpu_image_f64_matches_reference_fixture(ctx, path):
+    d = np.load(path)
+    for op in OPS:
+        got = ctx.image_morph_f64(int(d["width"]), int(d["height"]), d["offs"], d["events"], float(d["radius"]), op)
+        assert np.array_equal(got[0], d[f"{op}_offs"]) and np.array_equal(got[1], d[f"{op}_events"]), op
+
+
+@pytest.mark.gpu
+def test_gpu_image_f64_matches_oracle(ctx, oracle):
+    rng = np.random.default_rng(9)
+    for trial in range(16):
+        w, h = int(rng.integers(1, 400)), int(rng.integers(1, 300))
+        offs, ev = random_f64(w, h, int(rng.integers(1, 1 << 30)), int(rng.integers(0, 8)))
+        for op, r in (("dilation", float(rng.choice([0.0, 0.01, 0.05]))), ("erosion", float(rng.choice([0.0, 2.0, 6.5]))),
+                      ("opening", 0.02), ("closing", 0.03)):
+            got = ctx.image_morph_f64(w, h, offs, ev, r, op)
+            want = oracle.image_morph_f64(w, h, offs, ev, r, OPS[op])
+            assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1]), (trial, w, h, r, op)
+    for mask_rows in ([[]] * 5, [[0.0, 7.0]] * 5, [[0.0, 0.0], [7.0, 7.0], [2.0, 5.0], [], [0.0, 7.0]]):
+        offs = np.cumsum([0] + [len(r) for r in mask_rows]).astype(np.int32)
+        ev = np.array([v for r in mask_rows for v in r], np.float64)
+        for op in OPS:
+            got = ctx.image_morph_f64(7, len(mask_rows), offs, ev, 0.3, op)
+            want = oracle.image_morph_f64(7, len(mask_rows), offs, ev, 0.3, OPS[op])
+            assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1]), (mask_rows, op)

@@ -116,6 +116,8 @@ SIGNATURES = {
     "vo_volume_measure": (C.c_int, [_P, _P, C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
     "vo_image_morph": (C.c_int, [_P, C.c_int, C.c_double, C.c_int, C.c_int, C.POINTER(C.c_int32),
                                  C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_int64]),
+    "vo_image_morph_f64": (C.c_int, [_P, C.c_int, C.c_double, C.c_int, C.c_int, C.POINTER(C.c_int32),
+                                     C.POINTER(C.c_double), C.POINTER(C.c_int32), C.POINTER(C.c_double), C.c_int64]),
     "vo_xor_volume_noalloc": (C.c_int, [C.POINTER(_Grid), _P, _P, _P, _P, _P, C.POINTER(C.c_double)]),
     "vo_batch_create": (C.c_int, [_P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_int,
                                   C.POINTER(_P), C.POINTER(_P)]),
@@ -356,6 +358,24 @@ class Context:
                 cap = int(out_o[-1])
                 continue
             self._check(rc, "vo_image_morph")
+            return out_o, out_e[:int(out_o[-1])].copy()
+
+    def image_morph_f64(self, width: int, height: int, row_offs, events, radius: float, op: str = "dilation"):
+        """The FP64 twin (DoubleCompressedImage): returns (row_offs, events) of the result."""
+        ro = np.ascontiguousarray(row_offs, dtype=np.int32)
+        ev = np.ascontiguousarray(events, dtype=np.float64)
+        if ev.size == 0:
+            ev = np.zeros(1)
+        out_o = np.zeros(height + 1, np.int32)
+        cap = max(16, 2 * int(ro[-1]) + 4 * height)
+        while True:
+            out_e = np.zeros(cap)
+            rc = lib().vo_image_morph_f64(self.handle, OPS[op], float(radius), int(width), int(height), _i32p(ro),
+                                          _f64p(ev), _i32p(out_o), _f64p(out_e), cap)
+            if rc == VO_ERANGE and int(out_o[-1]) > cap:
+                cap = int(out_o[-1])
+                continue
+            self._check(rc, "vo_image_morph_f64")
             return out_o, out_e[:int(out_o[-1])].copy()
 
     def measure(self, v: Volume):

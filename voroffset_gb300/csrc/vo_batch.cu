@@ -67,6 +67,7 @@ struct DilPlan {
   int4 *col = nullptr;
   float4 *prec = nullptr;
   unsigned *dmask = nullptr;
+  int mask_bits = 32;
   unsigned int *maxbits = nullptr;
   int2 *pairs = nullptr;
   int *mid_list = nullptr, *mid_count = nullptr;
@@ -224,7 +225,7 @@ BatchVol batch_vol(const DilPlan &d, int *ovf) {
   BatchVol v;
   const vo_grid &g = d.in.grid;
   v.A = FastArgs{g.nx, g.ny, d.T->host.W, d.in.beg, d.in.end, (const double *)d.in.z, d.zf, d.T->Hf, d.T->H,
-                 d.pairs, d.npairs, d.E, d.col, d.prec, d.dmask};
+                 d.pairs, d.npairs, d.E, d.col, d.prec, d.dmask, d.mask_bits};
   v.obeg = d.out.beg;
   v.oend = d.out.end;
   v.oz = d.out.z;
@@ -403,7 +404,10 @@ int plan_dilation_round(vo_ctx *ctx, vo_batch *b, std::vector<DilPlan> &dils, bo
     rc = plan_alloc(ctx, b, &d.zf, 2 * (size_t)std::max<int64_t>(d.in.entries, 1));
     if (!rc) rc = plan_alloc(ctx, b, &d.E, 1);
     if (!rc) rc = plan_alloc(ctx, b, &d.col, (size_t)ncols);
-    if (!rc) rc = plan_alloc(ctx, b, &d.dmask, (size_t)4 * kDomLevels * ncols);
+    // mean segments per column of the input, exact for CSR inputs, the capacity's half for slots
+    const double mean_in = d.in.cap > 0 && d.in.owns ? d.in.cap * 0.5 : (double)d.in.entries / std::max(ncols, 1);
+    d.mask_bits = mask_bits_for(mean_in);
+    if (!rc) rc = plan_alloc(ctx, b, &d.dmask, mask_words((size_t)ncols, d.mask_bits));
     if (!rc) rc = plan_alloc(ctx, b, &d.prec, pairs.size());
     if (!rc) rc = plan_alloc(ctx, b, &d.mid_list, (size_t)ncols);
     if (!rc) rc = plan_alloc(ctx, b, &d.mid_count, 1);
@@ -419,11 +423,12 @@ int plan_dilation_round(vo_ctx *ctx, vo_batch *b, std::vector<DilPlan> &dils, bo
     float *zf = d.zf, *E = d.E;
     int4 *col = d.col;
     unsigned *dmask = d.dmask;
+    const int mbits = d.mask_bits;
     unsigned int *mb = d.maxbits;
     const float R = (float)b->radii[d.vol];
     const DomLevels L = d.T->host.dom;
-    record(b, 3, [in, zf, E, mb, R, col, dmask, L](cudaStream_t st) {
-      fast_prepare(st, in.grid.nx, in.grid.ny, in.beg, in.end, in.z, zf, mb, R, E, col, dmask, L);
+    record(b, 3, [in, zf, E, mb, R, col, dmask, mbits, L](cudaStream_t st) {
+      fast_prepare(st, in.grid.nx, in.grid.ny, in.beg, in.end, in.z, zf, mb, R, E, col, dmask, mbits, L);
     });
     // candidates per column ~ 4 x pairs x mean segments of the input (no sizer)
     const double segs = d.in.cap > 0 && d.in.owns ? d.in.cap * 0.5 : (double)d.in.entries / std::max(ncols, 1);

@@ -129,7 +129,11 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
   // direction "x-" = 0), else x - a ("x+" = 1); likewise y with S & 2
   // ("y-" = 2, "y+" = 3).
   const int ncols = A.nx * A.ny;
-#define MASK(DIR, LV, C) ((LV) < kDomLevels ? A.dmask[((DIR) * kDomLevels + (LV)) * ncols + (C)] : 0u)
+  const int mbits = A.mask_bits;
+#define MASK(DIR, LV, C)                                                                                \
+  ((LV) < kDomLevels ? (mbits == 16 ? (unsigned)static_cast<const unsigned short *>(A.dmask)[((DIR) * kDomLevels + (LV)) * ncols + (C)] \
+                                    : static_cast<const unsigned *>(A.dmask)[((DIR) * kDomLevels + (LV)) * ncols + (C)])        \
+                     : 0u)
 #define LOAD_ONE(OK, XS, YS, S, R, D)                                                                   \
   {                                                                                                     \
     const int c_ = (OK) ? (XS) + A.nx * (YS) : 0;                                                       \
@@ -163,8 +167,8 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
     // FP16 bounds of the pair's growths (rounded down) for the source tests
     const __half dhx_h = __float2half_rd(dhx), dhy_h = __float2half_rd(dhy);
     // Per source: [kb, ke) and the mask of its kept segments (bit j: segment
-    // kb + j); a source of more than 32 segments keeps all (m = 0, dense).
-    // A source of up to 32 segments that is dominated whole has an empty kept
+    // kb + j); a source of more than mbits segments keeps all (m = 0, dense).
+    // A source of up to mbits segments that is dominated whole has an empty kept
     // mask; a source of more segments (no masks) is tested with its column
     // widths.
 #define SRC(S, XS, YS, C, DM, KB, KE, M)                                                                \
@@ -172,12 +176,12 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
     KB = (C).x;                                                                                         \
     KE = (C).y;                                                                                         \
     const int ns_ = KE - KB;                                                                            \
-    if (ns_ > 32) {                                                                                     \
+    if (ns_ > mbits) {                                                                                  \
       const int4 cr_ = A.col[(XS) + A.nx * (YS)];                                                       \
       if (__hle(half_of((unsigned)cr_.z, (S) & 1), dhx_h) || __hle(half_of((unsigned)cr_.w, (S) & 2), dhy_h)) \
         KE = KB;                                                                                        \
     }                                                                                                   \
-    M = ns_ <= 32 ? ~(DM) & (ns_ == 32 ? 0xffffffffu : ((1u << ns_) - 1u)) : 0u;                        \
+    M = ns_ <= mbits ? ~(DM) & (ns_ == 32 ? 0xffffffffu : ((1u << ns_) - 1u)) : 0u;                    \
   }
     int kb0, ke0, kb1, ke1, kb2, ke2, kb3, ke3;
     unsigned m0, m1, m2, m3;
@@ -186,7 +190,7 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
     SRC(2, x - a, y + d, c2, d2, kb2, ke2, m2)
     SRC(3, x + a, y + d, c3, d3, kb3, ke3, m3)
 #undef SRC
-#define KEPT(KB, KE, M) ((KE) - (KB) > 32 ? (KE) - (KB) : __popc(M))
+#define KEPT(KB, KE, M) ((KE) - (KB) > mbits ? (KE) - (KB) : __popc(M))
     const int t0 = KEPT(kb0, ke0, m0), t1 = KEPT(kb1, ke1, m1), t2 = KEPT(kb2, ke2, m2), t3 = KEPT(kb3, ke3, m3);
 #undef KEPT
     const int total = t0 + t1 + t2 + t3;
@@ -208,7 +212,7 @@ __device__ int fast_column(const FastArgs &A, float E, int x, int y, float2 *sv,
       kbs = s == 0 ? kb0 : s == 1 ? kb1 : s == 2 ? kb2 : kb3;                                           \
       kend = s == 0 ? ke0 : s == 1 ? ke1 : s == 2 ? ke2 : ke3;                                          \
       ms = s == 0 ? m0 : s == 1 ? m1 : s == 2 ? m2 : m3;                                                \
-      dense = kend - kbs > 32;                                                                          \
+      dense = kend - kbs > mbits;                                                                       \
       kc = kbs;                                                                                         \
     }                                                                                                   \
     KN = -1;                                                                                            \
@@ -541,8 +545,8 @@ __global__ void k_dh_tables(int Dy, int W, const double *__restrict__ H, const i
 // over its segments (-inf for an empty column), stored as FP16 rounded up in
 // the column record col[c] = (beg, end, x- | x+ << 16, y- | y+ << 16).
 __global__ void k_dominance(int nx, int ny, const int32_t *__restrict__ beg, const int32_t *__restrict__ end,
-                            const float2 *__restrict__ zf, int4 *__restrict__ col, unsigned *__restrict__ dmask,
-                            const DomLevels L) {
+                            const float2 *__restrict__ zf, int4 *__restrict__ col, void *__restrict__ dmask,
+                            int mask_bits, const DomLevels L) {
   const int ncols = nx * ny;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncols) return;
@@ -560,7 +564,7 @@ __global__ void k_dominance(int nx, int ny, const int32_t *__restrict__ beg, con
   unsigned bits[4][kDomLevels];
   for (int k = 0; k < 4; ++k)
     for (int l = 0; l < kDomLevels; ++l) bits[k][l] = 0u;
-  const bool masked = k1 - k0 <= 32;
+  const bool masked = k1 - k0 <= mask_bits;
   for (int i = k0; i < k1; ++i) {
     // bounds of the exact values: an FP32 copy is within half an ulp of its
     // FP64 value, so the neighbouring floats enclose it
@@ -584,7 +588,11 @@ __global__ void k_dominance(int nx, int ny, const int32_t *__restrict__ beg, con
   }
   if (dmask)
     for (int k = 0; k < 4; ++k)
-      for (int l = 0; l < kDomLevels; ++l) dmask[(size_t)(k * kDomLevels + l) * ncols + c] = bits[k][l];
+      for (int l = 0; l < kDomLevels; ++l) {
+        const size_t idx = (size_t)(k * kDomLevels + l) * ncols + c;
+        if (mask_bits == 16) static_cast<unsigned short *>(dmask)[idx] = (unsigned short)bits[k][l];
+        else static_cast<unsigned *>(dmask)[idx] = bits[k][l];
+      }
   unsigned h[4];
   for (int k = 0; k < 4; ++k) h[k] = __half_as_ushort(__float2half_ru(cmax[k]));
   col[c] = make_int4(k0, k1, (int)(h[0] | (h[1] << 16)), (int)(h[2] | (h[3] << 16)));
@@ -823,7 +831,8 @@ int dilate_fast(vo_ctx *ctx, double R, const vo_volume *in, vo_volume **out, vo_
   rc = dalloc(ctx, &zf, (size_t)std::max<int64_t>(2 * in->nseg, 2));
   if (!rc) rc = dalloc(ctx, &dE, 1);
   if (!rc) rc = dalloc(ctx, &col, (size_t)ncols);
-  if (!rc) rc = dalloc(ctx, &dmask, (size_t)4 * kDomLevels * ncols);
+  const int mbits = mask_bits_for((double)in->nseg / std::max(ncols, 1));
+  if (!rc) rc = dalloc(ctx, &dmask, mask_words((size_t)ncols, mbits));
   if (!rc) rc = dalloc(ctx, &prec, pairs.size());
   if (!rc) rc = dalloc(ctx, &dmax, 1);
   if (!rc) rc = dalloc(ctx, &dpairs, pairs.size());
@@ -835,14 +844,14 @@ int dilate_fast(vo_ctx *ctx, double R, const vo_volume *in, vo_volume **out, vo_
     cudaMemcpyAsync(dpairs, pairs.data(), sizeof(int2) * pairs.size(), cudaMemcpyHostToDevice, ctx->stream);
     cudaMemsetAsync(ctx->d_flags, 0, 3 * sizeof(int), ctx->stream);  // [0] tier-2 list, [1] fatal, [2] FP64 list
     cudaEventRecord(ctx->ev[0], ctx->stream);
-    fast_prepare(ctx->stream, nx, ny, in->offs, in->offs + 1, in->z, zf, dmax, (float)R, dE, col, dmask,
+    fast_prepare(ctx->stream, nx, ny, in->offs, in->offs + 1, in->z, zf, dmax, (float)R, dE, col, dmask, mbits,
                  T->host.dom);
     fast_pair_records(ctx->stream, dpairs, (int)pairs.size(), *T, prec);
     ctx->launches += 4;
     cudaEventRecord(ctx->ev[1], ctx->stream);
   }
   FastArgs A{nx, ny, h.W, in->offs, in->offs + 1, (const double *)in->z, zf, T->Hf, T->H, dpairs,
-             (int)pairs.size(), dE, col, prec, dmask};
+             (int)pairs.size(), dE, col, prec, dmask, mbits};
   const dim3 blk(kFB, kFBY), grd((nx + kPatchX - 1) / kPatchX, (ny + kPatchY - 1) / kPatchY);
   // union capacity from the input's mean segment count per column (24, 32,
   // 48 or 64; dense inputs take 48 up to 24 segments per column, which keeps
@@ -943,14 +952,14 @@ std::vector<int2> fast_pairs(const Tables &h) {
 }
 
 void fast_prepare(cudaStream_t st, int nx, int ny, const int32_t *beg, const int32_t *end, const double2 *z,
-                  float *zf, unsigned int *maxbits, float R, float *E, int4 *col, unsigned *dmask,
+                  float *zf, unsigned int *maxbits, float R, float *E, int4 *col, void *dmask, int mask_bits,
                   const DomLevels &L) {
   const int ncols = nx * ny;
   cudaMemsetAsync(maxbits, 0, sizeof(unsigned int), st);
   k_to_f32_cols<<<(ncols + 255) / 256, 256, 0, st>>>(ncols, beg, end, (const double *)z, zf, maxbits);
   k_guard<<<1, 1, 0, st>>>(maxbits, R, E);
   k_dominance<<<(ncols + 127) / 128, 128, 0, st>>>(nx, ny, beg, end, reinterpret_cast<const float2 *>(zf), col,
-                                                    dmask, L);
+                                                    dmask, mask_bits, L);
 }
 
 void fast_pair_records(cudaStream_t st, const int2 *pairs, int npairs, const DeviceTables &T, float4 *prec) {

@@ -23,6 +23,17 @@ constexpr int kCapLarge = 2048;  // overflow re-run capacity per column
 // thresholds keep the pruning exact; t[0] = 0 and the others are quantiles of
 // the pairs' growths for the radius, so that levels fall where pairs are.
 constexpr int kDomLevels = 11;  // 15 in a pair record means "no level"
+// Segment dominance masks hold one bit per segment of columns with at most
+// mask_bits segments (16 or 32 per dilation: 16 when the input averages at
+// most kMask16MeanSegs segments per column — 0.02 % of the 2048^2 workload's
+// columns have more than 16 — else 32); a column with more takes the dense
+// path: every segment, with the whole-column width test.
+constexpr double kMask16MeanSegs = 8.0;
+inline int mask_bits_for(double mean_segments_per_column) {
+  return mean_segments_per_column <= kMask16MeanSegs ? 16 : 32;
+}
+// 32-bit words of the mask planes [4 directions][kDomLevels][ncols]
+inline size_t mask_words(size_t ncols, int bits) { return (4 * (size_t)kDomLevels * ncols * bits + 31) / 32; }
 struct DomLevels {
   float t[kDomLevels];
 };
@@ -194,10 +205,12 @@ struct FastArgs {
   // step, dH of a y step), both built by the fast_* helpers below.
   const int4 *col;
   const float4 *prec;
-  // Segment dominance masks [4 directions][kDomLevels][ncols]: bit j of a
-  // column with at most 32 segments is set when its segment j lies in a
-  // neighbour segment widened by the level's threshold.
-  const unsigned *dmask;
+  // Segment dominance masks [4 directions][kDomLevels][ncols] of mask_bits
+  // (16 or 32) bits: bit j of a column with at most mask_bits segments is set
+  // when its segment j lies in a neighbour segment widened by the level's
+  // threshold.
+  const void *dmask;
+  int mask_bits;
 };
 
 // One dilation of a batch (device array element of the persistent kernel).
@@ -228,7 +241,7 @@ std::vector<int2> fast_pairs(const Tables &h);
 // FP32 copies of the values of a slot volume, the guard band scalar, the
 // column records (ncols int4) and the dominance masks (4 * kDomLevels * ncols).
 void fast_prepare(cudaStream_t st, int nx, int ny, const int32_t *beg, const int32_t *end, const double2 *z,
-                  float *zf, unsigned int *maxbits, float R, float *E, int4 *col, unsigned *dmask,
+                  float *zf, unsigned int *maxbits, float R, float *E, int4 *col, void *dmask, int mask_bits,
                   const DomLevels &L);
 // Pair records (npairs float4) from the device tables of radius T.
 void fast_pair_records(cudaStream_t st, const int2 *pairs, int npairs, const DeviceTables &T, float4 *prec);

@@ -385,30 +385,42 @@ __global__ void __launch_bounds__(kBigThreads) k_pass2_big(int nx, int ny, const
   }
 }
 
+// Persistent: one wave of blocks pulls kBX x kBY tiles of output columns from
+// a work queue (raster order) until none is left. `queue` is zeroed before
+// each launch.
 template <bool FILL>
 __global__ void __launch_bounds__(kBX *kBY) k_brute(int nx, int ny, const int32_t *__restrict__ offs,
                                                     const double2 *__restrict__ z, DevTables t,
                                                     int32_t *__restrict__ counts,
                                                     const int32_t *__restrict__ ooffs,
-                                                    double2 *__restrict__ oz, OvfList ovf) {
+                                                    double2 *__restrict__ oz, OvfList ovf, int *queue) {
   extern __shared__ double smem[];
+  __shared__ int s_tile;
   const int nB = (t.Dy + 1) * (t.Dy + 1);
-  for (int i = threadIdx.x + blockDim.x * threadIdx.y; i < nB; i += blockDim.x * blockDim.y)
-    smem[i] = t.HB[i];
-  __syncthreads();
-  const int x = blockIdx.x * kBX + threadIdx.x;
-  const int y = blockIdx.y * kBY + threadIdx.y;
-  if (x >= nx || y >= ny) return;
-  const int c = x + nx * y;
-  double2 A[kCapSmall];
-  const int n = brute_column<FILL>(x, y, nx, ny, offs, z, t, smem, A, kCapSmall,
-                                   FILL ? oz + ooffs[c] : nullptr);
-  if (!FILL) {
-    if (n < 0) {
-      record_overflow(ovf, c);
-      counts[c] = 0;
-    } else {
-      counts[c] = n;
+  const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+  for (int i = tid; i < nB; i += blockDim.x * blockDim.y) smem[i] = t.HB[i];
+  const int tiles_x = (nx + kBX - 1) / kBX;
+  const int ntiles = tiles_x * ((ny + kBY - 1) / kBY);
+  for (;;) {
+    __syncthreads();  // the table is loaded; the previous tile's index has been read
+    if (tid == 0) s_tile = atomicAdd(queue, 1);
+    __syncthreads();
+    const int tile = s_tile;
+    if (tile >= ntiles) break;
+    const int x = (tile % tiles_x) * kBX + threadIdx.x;
+    const int y = (tile / tiles_x) * kBY + threadIdx.y;
+    if (x >= nx || y >= ny) continue;
+    const int c = x + nx * y;
+    double2 A[kCapSmall];
+    const int n = brute_column<FILL>(x, y, nx, ny, offs, z, t, smem, A, kCapSmall,
+                                     FILL ? oz + ooffs[c] : nullptr);
+    if (!FILL) {
+      if (n < 0) {
+        record_overflow(ovf, c);
+        counts[c] = 0;
+      } else {
+        counts[c] = n;
+      }
     }
   }
 }
@@ -1051,10 +1063,17 @@ int dilate(vo_ctx *ctx, int method, double R, const vo_volume *in_user, vo_volum
     }
     cudaFuncSetAttribute(k_brute<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shb);
     cudaFuncSetAttribute(k_brute<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shb);
+    // one wave of persistent blocks; d_flags[4] is the tile queue
+    int per_sm = 0, sms = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_brute<false>, kBX * kBY, shb);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    const int pgrid = std::max(1, per_sm) * std::max(1, sms);
+    int *queue = ctx->d_flags + 4;
     cudaMemsetAsync(ctx->d_flags, 0, 2 * sizeof(int), ctx->stream);
+    cudaMemsetAsync(queue, 0, sizeof(int), ctx->stream);
     cudaEventRecord(ctx->ev[4], ctx->stream);
-    k_brute<false><<<grd, blk, shb, ctx->stream>>>(nx, ny, in->offs, in->z, t, s.counts, nullptr,
-                                                   nullptr, ovf);
+    k_brute<false><<<pgrid, blk, shb, ctx->stream>>>(nx, ny, in->offs, in->z, t, s.counts, nullptr,
+                                                     nullptr, ovf, queue);
     k_brute_big<false><<<gbig, kBigThreads, 0, ctx->stream>>>(nx, ny, in->offs, in->z, t, s.counts,
                                                              nullptr, nullptr, ovf, s.big);
     ctx->launches += 2;
@@ -1067,8 +1086,9 @@ int dilate(vo_ctx *ctx, int method, double R, const vo_volume *in_user, vo_volum
     }
     if (!rc) {
       cudaEventRecord(ctx->ev[6], ctx->stream);
-      k_brute<true><<<grd, blk, shb, ctx->stream>>>(nx, ny, in->offs, in->z, t, nullptr, res->offs,
-                                                    res->z, ovf);
+      cudaMemsetAsync(queue, 0, sizeof(int), ctx->stream);
+      k_brute<true><<<pgrid, blk, shb, ctx->stream>>>(nx, ny, in->offs, in->z, t, nullptr, res->offs,
+                                                      res->z, ovf, queue);
       k_brute_big<true><<<gbig, kBigThreads, 0, ctx->stream>>>(nx, ny, in->offs, in->z, t, nullptr,
                                                               res->offs, res->z, ovf, s.big);
       ctx->launches += 2;

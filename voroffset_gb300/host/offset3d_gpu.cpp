@@ -4,8 +4,9 @@
 //   input (-i), -o output mesh, -j json, -d dexel size, -n num dexels (-1: use
 //   -d), -p padding, -t threads (recorded only), -r radius, -m method,
 //   -x operation, -f force overwrite, -u radius in mm.
-// Methods: gpu (FP32-guarded exact, default), gpu_separable (FP64 kernels),
-// gpu_brute (lattice-disc brute force).
+// Methods: gpu (FP32-guarded exact, default), gpu_envelope (the two envelope
+// sweeps in FP64), gpu_separable (the painter form, FP64 kernels), gpu_brute
+// (lattice-disc brute force).
 // Additions: -s/--save-volume FILE writes the output volume (the text format of
 // CompressedVolume::save, or the exact binary CSR dump when FILE ends in .csr);
 // --boxes writes six quads per dexel box instead of the boundary surface.
@@ -35,7 +36,7 @@ struct Args {
 [[noreturn]] void usage(const char *msg) {
   std::fprintf(stderr,
                "%s\nusage: offset3d_gpu input [-o out.obj] [-j out.json] [-d size] [-n num_dexels] [-p padding]\n"
-               "       [-r radius] [-m gpu|gpu_separable|gpu_brute] [-x noop|dilation|erosion|closing|opening]\n"
+               "       [-r radius] [-m gpu|gpu_envelope|gpu_separable|gpu_brute] [-x noop|dilation|erosion|closing|opening]\n"
                "       [-f] [-u] [-s volume.txt|volume.csr] [--boxes]\n",
                msg);
   std::exit(2);
@@ -79,6 +80,7 @@ int main(int argc, char **argv) {
   Args args = parse(argc, argv);
   int method;
   if (args.method == "gpu") method = VO_METHOD_FAST;
+  else if (args.method == "gpu_envelope") method = VO_METHOD_ENVELOPE;
   else if (args.method == "gpu_separable") method = VO_METHOD_SEPARABLE;
   else if (args.method == "gpu_brute") method = VO_METHOD_BRUTE;
   else usage(("invalid method: " + args.method).c_str());
