@@ -84,6 +84,7 @@ class ClockSampler:
         self.lines = []
 
     def start(self):
+        self.lines = []
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
@@ -529,8 +530,57 @@ def main():
     launches, kernel_ms, out_segs, mid = acc["launches"], acc["kernel_ms"], acc["out_segs"], acc["mid"]
     value = job_rate(world, ncols * args.steps, dev_ms / 1e3)
 
-    # ---------------- comparison arms on the same volume: the plain GPU method
-    # (FP64 separable, count then fill) and the single-volume FP32-guarded method
+    # ---------------- end-to-end arm (pinned host buffers through the C ABI), right after the
+    # device-resident arm and before the FP64 comparison arms, which hold the GPU busy for tens of seconds
+    pin_offs = torch.empty(offs.size, dtype=torch.int32, pin_memory=True).numpy()
+    pin_z = torch.empty(max(z.size, 2), dtype=torch.float64, pin_memory=True).numpy()
+    pin_offs[:] = offs
+    pin_z[:z.size] = z
+    out_offs = torch.empty(ncols + 1, dtype=torch.int32, pin_memory=True).numpy()
+    out_z = torch.empty(max(2 * out_segs, 2), dtype=torch.float64, pin_memory=True).numpy()
+
+    # host-clock split of a step: the upload call (asynchronous copies, offsets checked while they
+    # run), the morphology call (its own total_ms: plan, replay, outputs; it waits for the upload),
+    # the download (synchronous) and the frees
+    parts = {"upload_ms": 0.0, "morph_ms": 0.0, "morph_call_ms": 0.0, "download_ms": 0.0, "free_ms": 0.0}
+
+    def e2e_step():
+        t0 = time.perf_counter()
+        v = ctx.upload(grid, pin_offs, pin_z[:z.size])
+        t1 = time.perf_counter()
+        if args.method == "batched":
+            outs, tm = ctx.morph_batched([v], ["dilation"], [args.radius], "fast")
+            o = outs[0]
+        else:
+            o, tm = ctx.morph(v, "dilation", args.radius, args.method)
+        t2 = time.perf_counter()
+        n_o, n_z = ctx.download_into(o, out_offs, out_z)
+        t3 = time.perf_counter()
+        o.free()
+        v.free()
+        t4 = time.perf_counter()
+        for k, dt in (("upload_ms", t1 - t0), ("morph_call_ms", t2 - t1), ("download_ms", t3 - t2),
+                      ("free_ms", t4 - t3)):
+            parts[k] += dt * 1e3
+        parts["morph_ms"] += tm["total_ms"]
+        return 4 * n_o + 8 * n_z
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    barrier()
+    parts.update({k: 0.0 for k in parts})
+    clocks.start()
+    t0 = time.perf_counter()
+    d2h = 0
+    for _ in range(args.steps):
+        d2h = e2e_step()
+    barrier()
+    e2e_s = maxreduce(time.perf_counter() - t0)
+    e2e_clk = clocks.stop()
+    e2e = job_rate(world, ncols * args.steps, e2e_s)
+
+    # ---------------- comparison arms on the same volume: the plain GPU method (FP64 envelope
+    # sweeps), its painter form (FP64) and the single-volume FP32-guarded method
     arms = {}
     if args.method == "batched" and not args.no_arms:
         # the plain method is the separable scheme's sweeping envelope form in FP64; the painter form
@@ -549,37 +599,6 @@ def main():
         arms["batched_vs_painter"] = value / arms["painter_separable_fp64"]["value"]
         if not args.no_learned_arm:
             arms["learned_sizing_cyl4096"] = learned_sizing_arm(ctx, sizer, rank, world, timed)
-
-    # ---------------- end-to-end arm (pinned host buffers through the C ABI)
-    pin_offs = torch.empty(offs.size, dtype=torch.int32, pin_memory=True).numpy()
-    pin_z = torch.empty(max(z.size, 2), dtype=torch.float64, pin_memory=True).numpy()
-    pin_offs[:] = offs
-    pin_z[:z.size] = z
-    out_offs = torch.empty(ncols + 1, dtype=torch.int32, pin_memory=True).numpy()
-    out_z = torch.empty(max(2 * out_segs, 2), dtype=torch.float64, pin_memory=True).numpy()
-
-    def e2e_step():
-        v = ctx.upload(grid, pin_offs, pin_z[:z.size])
-        if args.method == "batched":
-            outs, _ = ctx.morph_batched([v], ["dilation"], [args.radius], "fast")
-            o = outs[0]
-        else:
-            o, _ = ctx.morph(v, "dilation", args.radius, args.method)
-        n_o, n_z = ctx.download_into(o, out_offs, out_z)
-        o.free()
-        v.free()
-        return 4 * n_o + 8 * n_z
-
-    for _ in range(max(1, args.warmup)):
-        e2e_step()
-    barrier()
-    t0 = time.perf_counter()
-    d2h = 0
-    for _ in range(args.steps):
-        d2h = e2e_step()
-    barrier()
-    e2e_s = maxreduce(time.perf_counter() - t0)
-    e2e = job_rate(world, ncols * args.steps, e2e_s)
 
     # ---------------- roofline of the dominant kernel
     kname = {"batched": "k_fast_batched", "fast": "k_fast", "separable": "k_pass2", "brute": "k_brute",
@@ -607,7 +626,8 @@ def main():
             "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic", "config": cfg, "run": run,
             "e2e": {"value": e2e, "unit": "Mcolumns/s", "h2d_bytes_per_step": int(in_bytes),
-                    "d2h_bytes_per_step": int(d2h)},
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3 / args.steps,
+                    "sm_mhz": e2e_clk.get("sm_mhz"), "split": {k: v / args.steps for k, v in parts.items()}},
             "gpu_launches": int(launches),
             "roofline": roofline, "clocks": clk, "arms": arms,
             "gsegments_per_s": world * (int(offs[-1]) + int(out_segs)) * args.steps / (dev_ms / 1e3) / 1e9}

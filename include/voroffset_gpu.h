@@ -106,7 +106,10 @@ void *vo_stream(vo_ctx *ctx);
 int vo_sync(vo_ctx *ctx);
 
 /* Volumes. Upload copies host CSR into a new device volume
- * (the value semantics of VoronoiMorpho::dilation's by-value input, Voronoi.h:18). */
+ * (the value semantics of VoronoiMorpho::dilation's by-value input, Voronoi.h:18).
+ * The copies run on the context's stream: from page-locked host memory they
+ * are asynchronous, so such buffers must stay unchanged until the next call
+ * that returns results (vo_morph, vo_volume_download, ...) has returned. */
 int vo_volume_upload(vo_ctx *ctx, const vo_grid *grid, const int32_t *offs, const double *z,
                      vo_volume **out);
 /* Grid and segment count of a volume (the size query before a download). */

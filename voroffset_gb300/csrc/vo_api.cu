@@ -280,21 +280,26 @@ int vo_volume_upload(vo_ctx *ctx, const vo_grid *grid, const int32_t *offs, cons
   *out = nullptr;
   const int64_t ncols = (int64_t)grid->nx * grid->ny;
   if (offs[0] != 0) return set_error(ctx, VO_EINVAL, "upload: offs[0] must be 0");
-  for (int64_t c = 0; c < ncols; ++c)
-    if (offs[c + 1] < offs[c]) return set_error(ctx, VO_EINVAL, "upload: offsets must not decrease");
   const int64_t nseg = offs[ncols];
+  if (nseg < 0) return set_error(ctx, VO_EINVAL, "upload: offsets must not decrease");
   if (nseg > 0 && !z) return set_error(ctx, VO_EINVAL, "upload: z is NULL");
   cudaSetDevice(ctx->device);
   vo_volume *v = nullptr;
   int rc = volume_alloc(ctx, *grid, nseg, &v);
   if (rc) return rc;
+  // The copies are issued first; the offsets are validated on the host while
+  // they run (the caller's z holds 2 * offs[ncols] values either way).
   cudaError_t e = cudaMemcpyAsync(v->offs, offs, sizeof(int32_t) * (ncols + 1),
                                   cudaMemcpyHostToDevice, ctx->stream);
   if (e == cudaSuccess && nseg > 0)
     e = cudaMemcpyAsync(v->z, z, sizeof(double) * 2 * nseg, cudaMemcpyHostToDevice, ctx->stream);
-  if (e != cudaSuccess) {
+  bool monotone = true;
+  for (int64_t c = 0; c < ncols; ++c) monotone &= offs[c + 1] >= offs[c];
+  if (e != cudaSuccess || !monotone) {
+    cudaStreamSynchronize(ctx->stream);
     vo_volume_free(ctx, v);
-    return cuda_error(ctx, e, "upload");
+    if (e != cudaSuccess) return cuda_error(ctx, e, "upload");
+    return set_error(ctx, VO_EINVAL, "upload: offsets must not decrease");
   }
   *out = v;
   return VO_OK;
