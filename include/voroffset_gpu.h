@@ -86,7 +86,9 @@ typedef struct {
   int64_t mid_pieces; /* pass-1 intermediate size (summed over chained ops) */
   int64_t out_segments;
   int32_t kernel_launches; /* kernels this call launched */
-  int32_t overflow_columns; /* columns re-run through the large-capacity path */
+  int32_t overflow_columns; /* columns re-run through the large-capacity path (envelope
+                             * form: lines and rows whose sweep ran with its state in
+                             * global memory) */
   /* device time (CUDA events on the context stream) of the pass-1 count,
    * pass-1 fill, pass-2 count and pass-2 fill kernels, summed over the call
    * (brute force: [2] count, [3] fill) */

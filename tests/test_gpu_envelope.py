@@ -52,6 +52,45 @@ def test_envelope_states_beyond_shared_memory(ctx, vo, oracle):
     got, t = run(ctx, grid, offs, z, "dilation", 4.0)
     assert_same(got, oracle.morph(ogrid(oracle, grid), offs, z, 4.0, "dilation"), tol=0.0)
     assert t["mid_pieces"] > 0  # the envelope kernels ran (the painter form reports its own pieces)
+    assert t["overflow_columns"] > 0  # lines or rows re-ran with global-memory state
+
+
+@pytest.mark.parametrize("cap", [48, 160])
+def test_envelope_rows_rerun_in_global_memory(ctx, vo, oracle, cap, monkeypatch):
+    """A lowered first-tier stadium capacity (VO_ENVELOPE_STATE_CAP) sends rows
+    of an ordinary volume to the re-run with global-memory state, which prunes
+    dominated stadiums the same way: results unchanged, re-runs counted."""
+    grid, offs, z = vo.synth_volume(vo.SynthSpec(80, ny=72, n_spheres=60, s_rmin=2, s_rmax=16, n_cyl=10, seed=93))
+    monkeypatch.setenv("VO_ENVELOPE_STATE_CAP", str(cap))
+    reruns = 0
+    for op, r in (("dilation", 9.0), ("erosion", 5.5), ("closing", 12.0)):
+        got, t = run(ctx, grid, offs, z, op, r)
+        reruns += t["overflow_columns"]
+        assert_same(got, oracle.morph(ogrid(oracle, grid), offs, z, r, op), tol=0.0, what=f"{op} cap={cap}")
+    assert reruns > 0
+
+
+def test_envelope_pruning_keeps_nested_plates(ctx, vo, oracle):
+    """Columns whose segments nest inside their neighbours' with margins just
+    above and just below what the chord growth allows: stadiums that a newer
+    piece holds for the rest of their lives leave the state, the others stay,
+    and the union equals the oracle's."""
+    nx, ny = 40, 12
+    rng = np.random.default_rng(7)
+    cols = []
+    for y in range(ny):
+        for x in range(nx):
+            base = 50.0 + 0.37 * ((x * 7 + y * 3) % 11)
+            w = 3.0 + 0.5 * np.sin(0.7 * x + 0.3 * y)
+            eps = rng.choice([-1e-9, 0.0, 1e-9, 0.25])
+            cols.append([base - eps, base + w + eps, base + w + 4.0, base + w + 4.0 + 0.5 * (x % 3)])
+    offs = (np.arange(nx * ny + 1) * 2).astype(np.int32)
+    z = np.asarray(cols, dtype=np.float64).reshape(-1)
+    grid = vo.Grid(nx, ny, (0, 0, 0), (nx, ny, 80), 1.0, 0)
+    for r in (3.0, 6.5, 11.0):
+        got, t = run(ctx, grid, offs, z, "dilation", r)
+        assert t["mid_pieces"] > 0
+        assert_same(got, oracle.morph(ogrid(oracle, grid), offs, z, r, "dilation"), tol=0.0, what=f"r={r}")
 
 
 @pytest.fixture(scope="module")

@@ -42,6 +42,7 @@
 // beyond even that, sends the whole volume to the painter form of the method
 // (VO_METHOD_SEPARABLE), which has no such limits.
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstdlib>
 #include <vector>
@@ -57,7 +58,7 @@ constexpr int kE1Cap = 448;          // shared-memory envelope capacity per line
 constexpr int kE1CapBig = 16384;     // global-memory capacity of the re-run
 constexpr int kE2Threads = 256;      // threads of a pass-2 block (one row)
 constexpr int kE2Stage = 768;        // staged pieces per column
-constexpr int kE2CapSmall = 3072;    // shared-memory stadium capacity of the first launch
+constexpr int kE2CapSmall = 4864;    // shared-memory stadium capacity of the first launch (227 KB in all)
 constexpr int kE2CapBig = 65536;     // global-memory stadium capacity of the re-run
 constexpr int kE2Out = 64;           // union intervals per column (output slot)
 constexpr int kWaitIters = 1 << 22;  // bounded mbarrier waits
@@ -390,15 +391,47 @@ struct E2Args {
   int *list;             // rows (band-relative) whose stadium set outgrew the shared capacity
   double2 *gz;           // re-run: 2 * kE2CapBig per block
   uint32_t *gk;          // re-run: keys, 2 * kE2CapBig per block
-  int *grank;            // re-run: kE2CapBig + 1 per block
+  double prune_eps;      // margin of the dominance test (a bound on the H tables' rounding)
+  int cap_small;         // stadium capacity of the first launch (<= kE2CapSmall)
+  int *ghist;            // placement counts of columns with more than kE2Stage pieces (per block)
+  int ghist_stride;      // ints per block of ghist (the band's most pieces per column + 2)
 };
+
+// Key of a stadium found dominated for the rest of its life: kept in place for
+// the column where it was found (no chord, no gap), dropped at the next one.
+constexpr uint32_t kDeadKey = 0xffffffffu;
 
 // A stadium (key: x0 | d << 24) reaches column x: d is a pass-1 label (<= Dy)
 // and the column lies within Dx[d] of x0 on the swept side.
 __device__ __forceinline__ bool live(uint32_t k, int x, int dir, const E2Args &A) {
+  if (k == kDeadKey) return false;
   const int d = (int)(k >> 24);
   const int age = dir == 0 ? x - (int)(k & 0xffffffu) : (int)(k & 0xffffffu) - x;
   return d <= A.Dy && age >= 0 && age <= __ldg(&A.Dx[d]);
+}
+
+// Whether the new piece p (label dp, entering at column x) holds the chord of
+// the live stadium v (key k) at every column the stadium still reaches, so
+// that the stadium can leave the state without changing any union.
+// With h_d(t) = sqrt(c_d - t^2), c_d = fl(r(d)^2), the tables hold
+// H[d][t] = fl(sqrt(fl(c_d - t^2))) within 1.6 * 2^-53 * R of h_d(t). For the
+// stadium (column xi, label di) and the piece, g(x') = h_dp(|x' - x|) -
+// h_di(|x' - xi|) has g' > 0 wherever g >= 0 (the piece is the younger one),
+// so g >= M' at x keeps g >= M' at every later column the piece outlives. With
+// M the larger of the core overhangs a_p - a_v, b_v - b_p (at least 0) and
+// M' = M + 4 table errors, the tables' chords at every later column satisfy
+// [a_v - H_v, b_v + H_v] inside [a_p - H_p, b_p + H_p] in exact arithmetic on
+// the FP64 values, hence also after each endpoint's rounding. The test takes M
+// rounded up, the table difference rounded down and prune_eps >= 2^-50 * R.
+__device__ __forceinline__ bool covers_for_life(double2 p, int dp, double2 v, uint32_t k, int x, int dir,
+                                                const E2Args &A) {
+  const int di = (int)(k >> 24), xi = (int)(k & 0xffffffu);
+  const int li = __ldg(&A.Dx[di]), lj = __ldg(&A.Dx[dp]);
+  if (dir == 0 ? x + lj < xi + li : x - lj > xi - li) return false;  // the piece expires first
+  const int age = dir == 0 ? x - xi : xi - x;
+  const double hv = __ldg(&A.H[di * A.W + age]), hp = __ldg(&A.H[dp * A.W]);
+  const double m = fmax(fmax(__dsub_ru(p.x, v.x), __dsub_ru(v.y, p.y)), 0.0);
+  return __dsub_rd(hp, hv) >= __dadd_ru(m, A.prune_eps);
 }
 
 // Block scans over kE2Threads threads (8 warps): exclusive sum, exclusive
@@ -501,32 +534,30 @@ __device__ int warp_union_two(const double2 *U1, int n1, const double2 *U2, int 
 }
 
 template <bool BIG>
-__global__ void __launch_bounds__(kE2Threads, 1) k_env2(E2Args A, int nrows_or_list) {
+__global__ void __launch_bounds__(kE2Threads, BIG ? 5 : 1) k_env2(E2Args A, int nrows_or_list) {
   extern __shared__ __align__(16) unsigned char e2_smem[];
   __shared__ uint64_t bar[2];
   __shared__ BlockScratch bs;
   __shared__ double2 U[kE2Out], U1[kE2Out], Mrg[2 * kE2Out];
+  __shared__ int s_hist[2 * kE2Stage + 2];
   __shared__ int s_abort, s_nu;
   const int tid = threadIdx.x;
-  const int cap = BIG ? kE2CapBig : kE2CapSmall;
-  // shared layout: staging (2 buffers), then (first launch) stadiums S and T, ranks
+  const int cap = BIG ? kE2CapBig : A.cap_small;
+  // shared layout: staging (2 buffers), then (first launch) stadiums S and T
   double2 *stage = reinterpret_cast<double2 *>(e2_smem);
   double2 *Sz, *Tz;
   uint32_t *Sk, *Tk;
-  int *rank;
   if (BIG) {
     Sz = A.gz + (size_t)blockIdx.x * 2 * kE2CapBig;
     Tz = Sz + kE2CapBig;
     Sk = A.gk + (size_t)blockIdx.x * 2 * kE2CapBig;
     Tk = Sk + kE2CapBig;
-    rank = A.grank + (size_t)blockIdx.x * (kE2CapBig + 1);
   } else {
     unsigned char *p = e2_smem + 2 * kE2Stage * sizeof(double2);
     Sz = reinterpret_cast<double2 *>(p);
-    Tz = Sz + cap;
-    Sk = reinterpret_cast<uint32_t *>(Tz + cap);
-    Tk = Sk + cap;
-    rank = reinterpret_cast<int *>(Tk + cap);
+    Tz = Sz + A.cap_small;
+    Sk = reinterpret_cast<uint32_t *>(Tz + A.cap_small);
+    Tk = Sk + A.cap_small;
   }
   int yrel;
   if (BIG) {
@@ -556,6 +587,7 @@ __global__ void __launch_bounds__(kE2Threads, 1) k_env2(E2Args A, int nrows_or_l
     };
     bool staged_cur = issue(xs, 0);
     int buf = 0;
+    int keep = 0;  // this thread's items live at x (counted by the previous column's chord loop)
     for (int x = xs; x != xe; x += step) {
       const int c = x + nx * y, bc = x + nx * yrel;
       const int kb = A.poff[bc], m = A.poff[bc + 1] - kb, f = A.nF[c], b = m - f;
@@ -576,18 +608,20 @@ __global__ void __launch_bounds__(kE2Threads, 1) k_env2(E2Args A, int nrows_or_l
       if (xn != xe) staged_next = issue(xn, buf ^ 1);
       const double2 *F = P, *B = P + f;  // the column's forward and backward pieces, each sorted
       const uint8_t *Fd = A.pd + kb, *Bd = A.pd + kb + f;
-      // ---- 1. survivors (within reach at x) and their ranks
+      // placement counts: bin c of F (0 <= c <= f) and bin f + 1 + c of B
+      const int nbins = f + b + 2;
+      int *hist = m <= kE2Stage ? s_hist : (A.ghist ? A.ghist + (size_t)blockIdx.x * A.ghist_stride : nullptr);
+      if (hist == nullptr || (m > kE2Stage && nbins > A.ghist_stride)) {
+        if (tid == 0) atomicExch(&A.flags[kFlagFatal], 1);
+        if (staged_next && tid == 0) mbar_wait(&bar[buf ^ 1], phase[buf ^ 1]);
+        return;
+      }
+      for (int h = tid; h < nbins; h += kE2Threads) hist[h] = 0;
+      // ---- 1. survivors (within reach at x): each thread's first rank
       const int L = (n + kE2Threads - 1) / kE2Threads;
       const int r0 = min(n, tid * L), r1 = min(n, r0 + L);
-      int keep = 0;
-      for (int i = r0; i < r1; ++i) keep += live(Sk[i], x, dir, A) ? 1 : 0;
       int nkeep;
-      int rk = block_excl_sum(keep, bs, nkeep);
-      for (int i = r0; i < r1; ++i) {
-        rank[i] = rk;
-        rk += live(Sk[i], x, dir, A) ? 1 : 0;
-      }
-      if (tid == kE2Threads - 1) rank[n] = nkeep;
+      const int rk0 = block_excl_sum(keep, bs, nkeep);
       const int nn = nkeep + m;
       if (nn > cap) {
         if (tid == 0) {
@@ -600,22 +634,60 @@ __global__ void __launch_bounds__(kE2Threads, 1) k_env2(E2Args A, int nrows_or_l
       __syncthreads();
       // ---- 2. merge survivors, forward pieces and backward pieces into T in (start, end) order
       // (ties: survivors, F, B)
-      for (int i = r0; i < r1; ++i) {
-        const uint32_t k = Sk[i];
-        if (live(k, x, dir, A)) {
-          const double2 v = Sz[i];
-          const int pos = rank[i] + count_lex_less(F, f, v) + count_lex_less(B, b, v);
-          Tz[pos] = Sz[i];
-          Tk[pos] = k;
+      // A survivor that one of the new pieces beside it (in core order) holds
+      // for the rest of its life is marked dead (covers_for_life). Its counts
+      // cF, cB of smaller pieces also place the pieces: F[j] follows exactly
+      // the survivors v with cF(v) <= j (v <= F[j], survivors first on ties),
+      // so bin cF of a count over the survivors, summed up to j, is the number
+      // of survivors before F[j]; likewise for B. No search over the state.
+      {
+        // the thread's items are in core order, so their counts of smaller pieces only grow: one
+        // binary search for the first survivor, then steps forward
+        int rk = rk0, cF = -1, cB = -1;
+        for (int i = r0; i < r1; ++i) {
+          const uint32_t k = Sk[i];
+          if (live(k, x, dir, A)) {
+            const double2 v = Sz[i];
+            if (cF < 0) {
+              cF = count_lex_less(F, f, v);
+              cB = count_lex_less(B, b, v);
+            } else {
+              while (cF < f && lex_less(F[cF], v)) ++cF;
+              while (cB < b && lex_less(B[cB], v)) ++cB;
+            }
+            const int pos = rk++ + cF + cB;
+            bool dom = cF > 0 && covers_for_life(F[cF - 1], Fd[cF - 1], v, k, x, dir, A);
+            dom = dom || (cF < f && covers_for_life(F[cF], Fd[cF], v, k, x, dir, A));
+            dom = dom || (cB > 0 && covers_for_life(B[cB - 1], Bd[cB - 1], v, k, x, dir, A));
+            dom = dom || (cB < b && covers_for_life(B[cB], Bd[cB], v, k, x, dir, A));
+            Tz[pos] = v;
+            Tk[pos] = dom ? kDeadKey : k;
+            atomicAdd(&hist[cF], 1);
+            atomicAdd(&hist[f + 1 + cB], 1);
+          }
         }
       }
+      __syncthreads();
+      {  // inclusive prefix sums of the bins (F's, then B's on top of all survivors)
+        const int K = (nbins + kE2Threads - 1) / kE2Threads;
+        const int h0 = min(nbins, tid * K), h1 = min(nbins, h0 + K);
+        int part = 0;
+        for (int h = h0; h < h1; ++h) part += hist[h];
+        int tot;
+        int run = block_excl_sum(part, bs, tot);
+        for (int h = h0; h < h1; ++h) {
+          run += hist[h];
+          hist[h] = run;
+        }
+      }
+      __syncthreads();
       for (int j = tid; j < m; j += kE2Threads) {
         const bool isF = j < f;
         const int jj = isF ? j : j - f;
         const double2 p = isF ? F[jj] : B[jj];
         const int d = isF ? Fd[jj] : Bd[jj];
-        const int pos =
-            jj + rank[count_lex_leq(Sz, n, p)] + (isF ? count_lex_less(B, b, p) : count_lex_leq(F, f, p));
+        const int before = isF ? hist[jj] : hist[f + 1 + jj] - hist[f];  // survivors before the piece
+        const int pos = jj + before + (isF ? count_lex_less(B, b, p) : count_lex_leq(F, f, p));
         Tz[pos] = p;
         Tk[pos] = (uint32_t)x | ((uint32_t)d << 24);
       }
@@ -631,13 +703,21 @@ __global__ void __launch_bounds__(kE2Threads, 1) k_env2(E2Args A, int nrows_or_l
       n = nn;
       // ---- 3. chords at x and their union (sort-free: prefix max of hi vs suffix min of lo); the
       // buffer T is free after the swap and holds (lo, hi), then (min lo over the later items, hi)
+      // (the same split of the items over the threads as step 1 of the next column, which takes
+      // its survivor counts from here)
       const int L2 = (n + kE2Threads - 1) / kE2Threads;
       const int q0 = min(n, tid * L2), q1 = min(n, q0 + L2);
       double run_max = -INFINITY, run_min = INFINITY;
+      keep = 0;
       for (int i = q0; i < q1; ++i) {
         const uint32_t k = Sk[i];
-        // every item here is live (d <= Dy, 0 <= age <= Dx[d] < W); the clamps only keep the table
-        // reads in bounds whatever the key holds
+        keep += live(k, x + step, dir, A) ? 1 : 0;
+        if (k == kDeadKey) {  // held by a new piece's chord: no chord of its own
+          Tz[i] = make_double2(INFINITY, -INFINITY);
+          continue;
+        }
+        // every other item here is live (d <= Dy, 0 <= age <= Dx[d] < W); the clamps only keep the
+        // table reads in bounds whatever the key holds
         const int d = min((int)(k >> 24), A.Dy);
         const int age = max(0, min(A.W - 1, dir == 0 ? x - (int)(k & 0xffffffu) : (int)(k & 0xffffffu) - x));
         const double h = __ldg(&A.H[d * A.W + age]);
@@ -659,13 +739,15 @@ __global__ void __launch_bounds__(kE2Threads, 1) k_env2(E2Args A, int nrows_or_l
         }
         if (q0 == 0 && q1 > 0) start0 = sm;  // min lo over all items
       }
+      // a gap follows item i when the items up to i end below every later start; dead items (no chord)
+      // and the live items after which only dead ones follow (no later start) have none
       int gaps = 0;
       {
         double pm = pmax0;
         for (int i = q0; i < q1; ++i) {
           const double2 t = Tz[i];
           pm = fmax(pm, t.y);
-          if (i + 1 < n && pm < t.x) ++gaps;
+          if (i + 1 < n && t.y != -INFINITY && t.x != INFINITY && pm < t.x) ++gaps;
         }
       }
       int G;
@@ -683,7 +765,7 @@ __global__ void __launch_bounds__(kE2Threads, 1) k_env2(E2Args A, int nrows_or_l
         for (int i = q0; i < q1; ++i) {
           const double2 t = Tz[i];
           pm = fmax(pm, t.y);
-          if (i + 1 < n && pm < t.x) {
+          if (i + 1 < n && t.y != -INFINITY && t.x != INFINITY && pm < t.x) {
             U[g].y = pm;
             U[g + 1].x = t.x;
             ++g;
@@ -732,9 +814,20 @@ __global__ void k_row_pieces(int nx, int ny, const int32_t *nF, const int32_t *n
   rows[y] = s;
 }
 
-__global__ void k_band_counts(int n, const int32_t *nF, const int32_t *nB, int32_t *cnt) {
+// Lists every row of a band for the global-memory sweep.
+__global__ void k_list_rows(int n, int *list, int *flags) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) cnt[i] = nF[i] + nB[i];
+  if (i < n) list[i] = i;
+  if (i == 0) flags[kFlagListed] = n;
+}
+
+// Pieces per column of a band, and their maximum (atomicMax into *maxc).
+__global__ void k_band_counts(int n, const int32_t *nF, const int32_t *nB, int32_t *cnt, int *maxc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int v = i < n ? nF[i] + nB[i] : 0;
+  if (i < n) cnt[i] = v;
+  const int w = __reduce_max_sync(0xffffffffu, v);
+  if ((threadIdx.x & 31) == 0) atomicMax(maxc, w);
 }
 
 size_t e1_smem_bytes(bool big) {
@@ -746,7 +839,7 @@ size_t e2_smem_bytes(bool big) {
   const size_t stage = 2 * (size_t)kE2Stage * sizeof(double2);
   if (big) return stage;
   const size_t cap = (size_t)kE2CapSmall;
-  return stage + 2 * cap * (sizeof(double2) + sizeof(uint32_t)) + (cap + 1) * sizeof(int);
+  return stage + 2 * cap * (sizeof(double2) + sizeof(uint32_t));
 }
 
 }  // namespace
@@ -761,6 +854,13 @@ int dilate_envelope(vo_ctx *ctx, double R, const vo_volume *in, vo_volume **out,
   int rc = get_tables(ctx, R, std::max(nx, ny), &T);
   if (rc) return rc;
   const int Dy = T->host.Dy, W = T->host.W;
+  // first-tier stadium capacity of pass 2; VO_ENVELOPE_STATE_CAP lowers it (tests use it to send
+  // rows to the global-memory re-run)
+  int cap2 = kE2CapSmall;
+  if (const char *sc = std::getenv("VO_ENVELOPE_STATE_CAP")) {
+    const int v = std::atoi(sc);
+    if (v > 0) cap2 = std::min(cap2, v);
+  }
   cudaFuncSetAttribute(k_env1<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e1_smem_bytes(false));
   cudaFuncSetAttribute(k_env1<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e1_smem_bytes(false));
   cudaFuncSetAttribute(k_env2<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e2_smem_bytes(false));
@@ -776,14 +876,14 @@ int dilate_envelope(vo_ctx *ctx, double R, const vo_volume *in, vo_volume **out,
   if (!rc) rc = dalloc(ctx, &slots, (size_t)ncols * kE2Out);
   double2 *gz1 = nullptr, *gz2 = nullptr;
   int gz1_lines = 0;
-  int *gl1 = nullptr, *grank = nullptr;
+  int *gl1 = nullptr, *ghist = nullptr;
   uint32_t *gk2 = nullptr;
   int32_t *poff = nullptr;
   double2 *pz = nullptr;
   uint8_t *pd = nullptr;
   vo_volume *res = nullptr;
   int fallback = 0;
-  int hflags[3] = {0, 0, 0};
+  int hflags[4] = {0, 0, 0, 0};  // status words, then (slot 3) the band's most pieces per column
   auto flags_now = [&]() -> int {
     VO_CK(ctx, cudaMemcpyAsync(hflags, ctx->d_flags, sizeof(hflags), cudaMemcpyDeviceToHost, ctx->stream));
     VO_CK(ctx, cudaStreamSynchronize(ctx->stream));
@@ -805,6 +905,7 @@ int dilate_envelope(vo_ctx *ctx, double R, const vo_volume *in, vo_volume **out,
     // lines listed by the first launch run again with their envelope in global memory
     const int nl = hflags[kFlagListed];
     if (nl == 0 || hflags[kFlagFatal]) return VO_OK;
+    if (!a.pz) ctx->ovf_cols += nl;  // counted once, in the count pass
     if (nl > gz1_lines) {
       dfree(ctx, gz1);
       dfree(ctx, gl1);
@@ -867,11 +968,17 @@ int dilate_envelope(vo_ctx *ctx, double R, const vo_volume *in, vo_volume **out,
     long long ptotal = 0;
     rc = dalloc(ctx, &poff, (size_t)bcols + 1);
     if (!rc) {
+      cudaMemsetAsync(ctx->d_flags + 3, 0, sizeof(int), ctx->stream);
       k_band_counts<<<(bcols + 255) / 256, 256, 0, ctx->stream>>>(bcols, nF + (size_t)yb0 * nx,
-                                                                  nB + (size_t)yb0 * nx, bcnt);
+                                                                  nB + (size_t)yb0 * nx, bcnt, ctx->d_flags + 3);
       ctx->launches += 1;
       rc = scan_counts(ctx, bcnt, poff, bcols, &ptotal);
     }
+    if (!rc) rc = flags_now();
+    // placement counts of columns beyond the staging buffer live in global memory, one range per block
+    const int max_pieces = hflags[3];
+    const int hstride = max_pieces > kE2Stage ? max_pieces + 2 : 0;
+    if (!rc && hstride > 0) rc = dalloc(ctx, &ghist, (size_t)hstride * (yb1 - yb0));
     if (!rc) rc = dalloc(ctx, &pz, (size_t)ptotal);
     if (!rc) rc = dalloc(ctx, &pd, (size_t)ptotal);
     if (rc) break;
@@ -895,31 +1002,37 @@ int dilate_envelope(vo_ctx *ctx, double R, const vo_volume *in, vo_volume **out,
     if (!rc && hflags[kFlagFatal]) fallback = 1;
     cudaEventRecord(e1, ctx->stream);
     if (!rc && !fallback) {
-      E2Args a2{nx, yb0, Dy, W, T->H, T->Dx, poff, nF, pz, pd, slots, counts, ctx->d_flags, list, nullptr,
-                nullptr, nullptr};
+      E2Args a2{nx,    yb0,    Dy,      W,  T->H, T->Dx, poff, nF, pz, pd, slots, counts, ctx->d_flags, list,
+                nullptr, nullptr, std::ldexp(std::max(R, 1.0), -46), cap2, ghist, hstride};
       cudaMemsetAsync(ctx->d_flags, 0, 3 * sizeof(int), ctx->stream);
-      k_env2<false><<<yb1 - yb0, kE2Threads, e2_smem_bytes(false), ctx->stream>>>(a2, yb1 - yb0);
+      // Rows whose live-stadium state would mostly outgrow shared memory go straight to the
+      // global-memory sweep, which runs five rows per SM against one: the state is estimated as a
+      // third of the pieces of the floor(R) + 1 columns within reach (what the pruning leaves on
+      // the 2048^2 and 1024^2 sphere workloads at r = 32).
+      const double mean_pieces = bcols > 0 ? (double)ptotal / bcols : 0.0;
+      if (mean_pieces * (Dy + 1) / 3.0 > 0.6 * cap2) {
+        k_list_rows<<<(yb1 - yb0 + 255) / 256, 256, 0, ctx->stream>>>(yb1 - yb0, list, ctx->d_flags);
+      } else {
+        k_env2<false><<<yb1 - yb0, kE2Threads, e2_smem_bytes(false), ctx->stream>>>(a2, yb1 - yb0);
+      }
       ctx->launches += 1;
       rc = flags_now();
       const int nl = hflags[kFlagListed];
+      ctx->ovf_cols += nl;
       if (!rc && !hflags[kFlagFatal] && nl > 0) {
         rc = dalloc(ctx, &gz2, (size_t)2 * kE2CapBig * nl);
         if (!rc) rc = dalloc(ctx, &gk2, (size_t)2 * kE2CapBig * nl);
-        if (!rc) rc = dalloc(ctx, &grank, (size_t)(kE2CapBig + 1) * nl);
         if (!rc) {
           a2.gz = gz2;
           a2.gk = gk2;
-          a2.grank = grank;
           k_env2<true><<<nl, kE2Threads, e2_smem_bytes(true), ctx->stream>>>(a2, 0);
           ctx->launches += 1;
           rc = flags_now();
         }
         dfree(ctx, gz2);
         dfree(ctx, gk2);
-        dfree(ctx, grank);
         gz2 = nullptr;
         gk2 = nullptr;
-        grank = nullptr;
       }
       if (!rc && hflags[kFlagFatal]) fallback = 1;
     }
@@ -936,9 +1049,11 @@ int dilate_envelope(vo_ctx *ctx, double R, const vo_volume *in, vo_volume **out,
     dfree(ctx, poff);
     dfree(ctx, pz);
     dfree(ctx, pd);
+    dfree(ctx, ghist);
     poff = nullptr;
     pz = nullptr;
     pd = nullptr;
+    ghist = nullptr;
   }
   // ---- output
   long long total = 0;
@@ -978,6 +1093,7 @@ int dilate_envelope(vo_ctx *ctx, double R, const vo_volume *in, vo_volume **out,
   dfree(ctx, poff);
   dfree(ctx, pz);
   dfree(ctx, pd);
+  dfree(ctx, ghist);
   if (rc || fallback) {
     if (res) vo_volume_free(ctx, res);
     if (!rc && hflags[kFlagTimeout]) return set_error(ctx, VO_ETIMEOUT, "envelope: a staged copy did not arrive");
