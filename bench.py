@@ -134,16 +134,16 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def traffic_per_column(kernel: str, radius: float):
-    """DRAM bytes per output column of a kernel from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", "dram_traffic.json")
+def kernel_counters(kernel: str, workload: str, radius: float) -> dict:
+    """Per-output-column ncu counters of a kernel on this workload and radius from the committed
+    summary (DRAM bytes, warp and thread instructions), or {} when none was captured."""
+    path = os.path.join(ROOT, "profiles", "kernel_counters.json")
     try:
         with open(path) as fh:
-            d = json.load(fh)
-        e = d.get(f"{kernel}@r{int(radius)}")
-        return None if e is None else float(e["bytes_per_column"])
+            e = json.load(fh).get(f"{kernel}@r{int(radius)}")
+        return e if e and str(e.get("workload", "")).startswith(workload + " ") else {}
     except Exception:
-        return None
+        return {}
 
 
 def cpu_sample(grid, offs, z, radius, target_s, step_rows=None, gpu_out=None):
@@ -607,12 +607,27 @@ def main():
     alg_bytes = 4 * (ncols + 1) + 16 * int(offs[-1]) + 4 * (ncols + 1) + 16 * int(out_segs)
     peak, peak_kind = peaks()
     achieved = alg_bytes / (per_launch / 1e3) / 1e9 if per_launch > 0 else 0.0
-    tpc = traffic_per_column(kname, args.radius)
+    kc = kernel_counters(kname, args.workload, args.radius)
+    tpc = kc.get("bytes_per_column")
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": None if tpc is None else tpc * ncols,
                 "kernel": kname, "kernel_ms": per_launch, "peak_source": peak_kind,
                 "algorithmic_bytes": alg_bytes,
                 "op_achieved": alg_bytes / (dev_ms / args.steps / 1e3) / 1e9}
+    # the compute side: the kernel's instruction issue against the SMs' issue slots (4 schedulers per
+    # SM, one warp instruction per cycle each, at the median SM clock seen in the timed region), from
+    # the instruction counts of the committed ncu capture of this workload and the live kernel time
+    issue = None
+    wpc = kc.get("warp_instructions_per_column")
+    if wpc and per_launch > 0 and clk.get("sm_mhz"):
+        import torch
+        sms = torch.cuda.get_device_properties(local).multi_processor_count
+        ach = wpc * ncols / (per_launch / 1e3) / 1e9
+        pk = sms * 4 * clk["sm_mhz"] * 1e6 / 1e9
+        lanes = kc["thread_instructions_per_column"] / wpc
+        issue = {"bound": "issue", "achieved": ach, "peak": pk, "unit": "Gwarp-inst/s", "frac": ach / pk,
+                 "lanes_per_inst": lanes, "lane_weighted_frac": ach / pk * lanes / 32,
+                 "warp_inst_per_launch": wpc * ncols, "sms": sms, "source": kc.get("source")}
 
     dtype = "f64" if args.method in ("separable", "brute", "envelope") else "f32+f64"
     cfg = bench_config(args, grid, offs)
@@ -629,7 +644,7 @@ def main():
                     "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3 / args.steps,
                     "sm_mhz": e2e_clk.get("sm_mhz"), "split": {k: v / args.steps for k, v in parts.items()}},
             "gpu_launches": int(launches),
-            "roofline": roofline, "clocks": clk, "arms": arms,
+            "roofline": roofline, "issue_roofline": issue, "clocks": clk, "arms": arms,
             "gsegments_per_s": world * (int(offs[-1]) + int(out_segs)) * args.steps / (dev_ms / 1e3) / 1e9}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
