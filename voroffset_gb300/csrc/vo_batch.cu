@@ -287,7 +287,7 @@ int sm_count() {
 
 // Autotuner: times every (union capacity, register budget, block shape,
 // persistent or one block per item) on a sample of the round's queue (four evenly spaced
-// contiguous runs, about 1/16 of it and at least 512 items), the second tier
+// contiguous runs, about 1/16 of it but two to four waves of resident blocks, at least 512 items), the second tier
 // included, and keeps the fastest per column. Results are cached in the
 // context per (one dilation or several, log2 columns, radius bucket, dense or
 // not, learned or not).
@@ -334,9 +334,11 @@ int tune_shape(vo_ctx *ctx, vo_batch *b, const std::vector<DilPlan> &dils, const
     // together as in the real launch, so the sample sees its cache reuse
     const std::vector<int2> full = build_queue(dils, fby);
     // at least two waves of resident blocks: a sample smaller than a wave
-    // times the tail of a partly idle GPU, not the throughput of a full one
+    // times the tail of a partly idle GPU, not the throughput of a full one;
+    // at most four (or 1/16 of the queue when that is less), so that tuning a
+    // large dense round (4096^2 cylinders: 48 samples) stays a fraction of a second per sample
     const size_t waves = (size_t)2 * sms * per_sm;
-    const size_t want = std::min(full.size(), std::max<size_t>({512, full.size() / 16, waves}));
+    const size_t want = std::min(full.size(), std::max<size_t>({512, std::min(full.size() / 16, 2 * waves), waves}));
     std::vector<int2> sample;
     for (int r = 0; r < 4; ++r) {
       const size_t len = want / 4 + (r < (int)(want % 4) ? 1 : 0);
