@@ -434,8 +434,8 @@ __device__ __forceinline__ bool covers_for_life(double2 p, int dp, double2 v, ui
   return __dsub_rd(hp, hv) >= __dadd_ru(m, A.prune_eps);
 }
 
-// Block scans over kE2Threads threads (8 warps): exclusive sum, exclusive
-// prefix maximum (thread order) and exclusive suffix minimum (reverse order).
+// Block scans over kE2Threads threads (8 warps): exclusive sum, and the
+// exclusive prefix maximum with the exclusive suffix minimum.
 struct BlockScratch {
   int isum[kE2Threads / 32];
   double dmax[kE2Threads / 32], dmin[kE2Threads / 32];
@@ -461,38 +461,30 @@ __device__ __forceinline__ int block_excl_sum(int v, BlockScratch &s, int &total
   return pre + x - v;
 }
 
-__device__ __forceinline__ double block_excl_prefix_max(double v, BlockScratch &s) {
+// Exclusive prefix maximum of vmax (thread order) and exclusive suffix
+// minimum of vmin (reverse order), with one pair of barriers.
+__device__ __forceinline__ void block_excl_max_min(double vmax, double vmin, BlockScratch &s, double &pmax,
+                                                   double &smin) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  double x = v;
+  double x = vmax, y = vmin;
   for (int o = 1; o < 32; o <<= 1) {
-    const double y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o) x = fmax(x, y);
+    const double a = __shfl_up_sync(0xffffffffu, x, o);
+    const double b = __shfl_down_sync(0xffffffffu, y, o);
+    if (lane >= o) x = fmax(x, a);
+    if (lane + o < 32) y = fmin(y, b);
   }
   if (lane == 31) s.dmax[w] = x;
-  double ex = __shfl_up_sync(0xffffffffu, x, 1);
+  if (lane == 0) s.dmin[w] = y;
+  double ex = __shfl_up_sync(0xffffffffu, x, 1), ey = __shfl_down_sync(0xffffffffu, y, 1);
   if (lane == 0) ex = -INFINITY;
+  if (lane == 31) ey = INFINITY;
   __syncthreads();
-  double pre = -INFINITY;
+  double pre = -INFINITY, suf = INFINITY;
   for (int k = 0; k < w; ++k) pre = fmax(pre, s.dmax[k]);
-  __syncthreads();
-  return fmax(pre, ex);
-}
-
-__device__ __forceinline__ double block_excl_suffix_min(double v, BlockScratch &s) {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  double x = v;
-  for (int o = 1; o < 32; o <<= 1) {
-    const double y = __shfl_down_sync(0xffffffffu, x, o);
-    if (lane + o < 32) x = fmin(x, y);
-  }
-  if (lane == 0) s.dmin[w] = x;
-  double ex = __shfl_down_sync(0xffffffffu, x, 1);
-  if (lane == 31) ex = INFINITY;
-  __syncthreads();
-  double suf = INFINITY;
   for (int k = w + 1; k < kE2Threads / 32; ++k) suf = fmin(suf, s.dmin[k]);
   __syncthreads();
-  return fmin(suf, ex);
+  pmax = fmax(pre, ex);
+  smin = fmin(suf, ey);
 }
 
 // Union of the sorted (by lower end) interval lists U1[0..n1) and U2[0..n2)
@@ -727,8 +719,8 @@ __global__ void __launch_bounds__(kE2Threads, BIG ? 5 : 1) k_env2(E2Args A, int 
         run_max = fmax(run_max, hi);
         run_min = fmin(run_min, lo);
       }
-      const double pmax0 = block_excl_prefix_max(run_max, bs);
-      const double smin_after = block_excl_suffix_min(run_min, bs);
+      double pmax0, smin_after;
+      block_excl_max_min(run_max, run_min, bs, pmax0, smin_after);
       double start0 = INFINITY;
       {
         double sm = smin_after;
@@ -1005,12 +997,15 @@ int dilate_envelope(vo_ctx *ctx, double R, const vo_volume *in, vo_volume **out,
       E2Args a2{nx,    yb0,    Dy,      W,  T->H, T->Dx, poff, nF, pz, pd, slots, counts, ctx->d_flags, list,
                 nullptr, nullptr, std::ldexp(std::max(R, 1.0), -46), cap2, ghist, hstride};
       cudaMemsetAsync(ctx->d_flags, 0, 3 * sizeof(int), ctx->stream);
-      // Rows whose live-stadium state would mostly outgrow shared memory go straight to the
-      // global-memory sweep, which runs five rows per SM against one: the state is estimated as a
-      // third of the pieces of the floor(R) + 1 columns within reach (what the pruning leaves on
-      // the 2048^2 and 1024^2 sphere workloads at r = 32).
+      // The global-memory sweep runs five rows per SM against one in shared memory (227 KB per
+      // block); with at least two rows per SM to run it is the faster one (1024^2 spheres, r = 16:
+      // 389 against 467 ms), and so it is for rows whose live-stadium state would mostly outgrow
+      // shared memory, estimated as a third of the pieces of the floor(R) + 1 columns within reach
+      // (what the pruning leaves on the 2048^2 and 1024^2 sphere workloads at r = 32).
       const double mean_pieces = bcols > 0 ? (double)ptotal / bcols : 0.0;
-      if (mean_pieces * (Dy + 1) / 3.0 > 0.6 * cap2) {
+      int sms = 0;
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+      if (yb1 - yb0 >= 2 * std::max(sms, 1) || mean_pieces * (Dy + 1) / 3.0 > 0.6 * cap2) {
         k_list_rows<<<(yb1 - yb0 + 255) / 256, 256, 0, ctx->stream>>>(yb1 - yb0, list, ctx->d_flags);
       } else {
         k_env2<false><<<yb1 - yb0, kE2Threads, e2_smem_bytes(false), ctx->stream>>>(a2, yb1 - yb0);
