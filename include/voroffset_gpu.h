@@ -61,7 +61,10 @@ extern "C" {
  *   segments (Voronoi2D.cpp:591-723), pass 2 sweeps each row keeping the live
  *   stadiums of the pass-1 pieces and takes their union on every line
  *   (SeparatePower2D.cpp:228-541), one warp per line / one block per row.
- *   Same results as VO_METHOD_SEPARABLE. */
+ *   Same results as VO_METHOD_SEPARABLE. Environment: VO_ENVELOPE_BAND_PIECES
+ *   caps the pass-1 pieces held at once (rows are then swept in bands);
+ *   VO_ENVELOPE_STATE_CAP lowers the shared-memory stadium capacity of
+ *   pass 2 (rows beyond it sweep with global-memory state). */
 #define VO_METHOD_SEPARABLE 0
 #define VO_METHOD_BRUTE 1
 #define VO_METHOD_FAST 2
