@@ -34,13 +34,18 @@
 // (the reference's unionMap, HalfDilationOperator.hpp:5-15) by a warp
 // merge-path and the same scan. The result is the union of the same candidate
 // intervals as the reference's, computed with its FP64 expressions, so it is
-// bit-identical to the oracle.
+// bit-identical to the oracle. Pass 2 also drops stadiums that a newer piece
+// holds for the rest of their lives (covers_for_life): exact, and the state
+// shrinks about threefold.
 //
-// Capacities: the first launch keeps each state in shared memory; lines or
-// rows whose state outgrows it are listed and re-run with their state in
-// global memory. A column whose union outgrows its output slot, or a state
-// beyond even that, sends the whole volume to the painter form of the method
-// (VO_METHOD_SEPARABLE), which has no such limits.
+// Capacities: pass 1's first launch keeps each line's state in shared memory,
+// and lines whose state outgrows it re-run with it in global memory. Pass 2
+// does the same for bands of few rows; bands of at least two rows per SM, or
+// whose state is estimated beyond shared memory, sweep with global-memory
+// state from the start (five rows per SM against one). A column whose union
+// outgrows its output slot, or a state beyond the global capacity, sends the
+// whole volume to the painter form of the method (VO_METHOD_SEPARABLE), which
+// has no such limits.
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
