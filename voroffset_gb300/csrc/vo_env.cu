@@ -653,10 +653,16 @@ __global__ void __launch_bounds__(kE2Threads, BIG ? 5 : 1) k_env2(E2Args A, int 
               while (cB < b && lex_less(B[cB], v)) ++cB;
             }
             const int pos = rk++ + cF + cB;
-            bool dom = cF > 0 && covers_for_life(F[cF - 1], Fd[cF - 1], v, k, x, dir, A);
-            dom = dom || (cF < f && covers_for_life(F[cF], Fd[cF], v, k, x, dir, A));
-            dom = dom || (cB > 0 && covers_for_life(B[cB - 1], Bd[cB - 1], v, k, x, dir, A));
-            dom = dom || (cB < b && covers_for_life(B[cB], Bd[cB], v, k, x, dir, A));
+            // tested on every other column: a stadium the pieces of one column hold is mostly held by
+            // the next column's as well (2048^2 spheres + cylinders, r = 32: 3.86 s testing every
+            // column, 3.34 s every other one, 3.41 s every fourth; two candidates instead of four: 3.55 s)
+            bool dom = false;
+            if ((x & 1) == 0) {
+              dom = cF > 0 && covers_for_life(F[cF - 1], Fd[cF - 1], v, k, x, dir, A);
+              dom = dom || (cF < f && covers_for_life(F[cF], Fd[cF], v, k, x, dir, A));
+              dom = dom || (cB > 0 && covers_for_life(B[cB - 1], Bd[cB - 1], v, k, x, dir, A));
+              dom = dom || (cB < b && covers_for_life(B[cB], Bd[cB], v, k, x, dir, A));
+            }
             Tz[pos] = v;
             Tk[pos] = dom ? kDeadKey : k;
             atomicAdd(&hist[cF], 1);
