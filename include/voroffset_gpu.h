@@ -64,7 +64,8 @@ extern "C" {
  *   Same results as VO_METHOD_SEPARABLE. Environment: VO_ENVELOPE_BAND_PIECES
  *   caps the pass-1 pieces held at once (rows are then swept in bands);
  *   VO_ENVELOPE_STATE_CAP lowers the shared-memory stadium capacity of
- *   pass 2 (rows beyond it sweep with global-memory state). */
+ *   pass 2 (rows beyond it sweep with global-memory state);
+ *   VO_ENVELOPE_ROW_CHUNK caps the rows of one global-memory launch. */
 #define VO_METHOD_SEPARABLE 0
 #define VO_METHOD_BRUTE 1
 #define VO_METHOD_FAST 2

@@ -70,6 +70,19 @@ def test_envelope_rows_rerun_in_global_memory(ctx, vo, oracle, cap, monkeypatch)
     assert reruns > 0
 
 
+def test_envelope_global_sweep_in_row_chunks(ctx, vo, oracle, monkeypatch):
+    """The global-memory sweep launched over a few rows at a time
+    (VO_ENVELOPE_ROW_CHUNK), every row sent there (VO_ENVELOPE_STATE_CAP):
+    results unchanged."""
+    grid, offs, z = vo.synth_volume(vo.SynthSpec(72, ny=45, n_spheres=50, s_rmin=2, s_rmax=12, n_cyl=6, seed=95))
+    monkeypatch.setenv("VO_ENVELOPE_STATE_CAP", "16")
+    monkeypatch.setenv("VO_ENVELOPE_ROW_CHUNK", "7")
+    for op, r in (("dilation", 6.5), ("opening", 4.0)):
+        got, t = run(ctx, grid, offs, z, op, r)
+        assert t["overflow_columns"] > 0
+        assert_same(got, oracle.morph(ogrid(oracle, grid), offs, z, r, op), tol=0.0, what=op)
+
+
 def test_envelope_pruning_keeps_nested_plates(ctx, vo, oracle):
     """Columns whose segments nest inside their neighbours' with margins just
     above and just below what the chord growth allows: stadiums that a newer

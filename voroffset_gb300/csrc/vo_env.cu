@@ -558,7 +558,7 @@ __global__ void __launch_bounds__(kE2Threads, BIG ? 5 : 1) k_env2(E2Args A, int 
   }
   int yrel;
   if (BIG) {
-    if ((int)blockIdx.x >= A.flags[kFlagListed]) return;
+    if ((int)blockIdx.x >= nrows_or_list) return;
     yrel = A.list[blockIdx.x];
   } else {
     yrel = blockIdx.x;
@@ -1026,12 +1026,25 @@ int dilate_envelope(vo_ctx *ctx, double R, const vo_volume *in, vo_volume **out,
       const int nl = hflags[kFlagListed];
       ctx->ovf_cols += nl;
       if (!rc && !hflags[kFlagFatal] && nl > 0) {
-        rc = dalloc(ctx, &gz2, (size_t)2 * kE2CapBig * nl);
-        if (!rc) rc = dalloc(ctx, &gk2, (size_t)2 * kE2CapBig * nl);
-        if (!rc) {
-          a2.gz = gz2;
-          a2.gk = gk2;
-          k_env2<true><<<nl, kE2Threads, e2_smem_bytes(true), ctx->stream>>>(a2, 0);
+        // the listed rows sweep with global-memory state (2.6 MB per row), in chunks of rows whose
+        // state fits a quarter of the free device memory
+        size_t freeb = 0, totb = 0;
+        cudaMemGetInfo(&freeb, &totb);
+        const size_t per_row = (size_t)2 * kE2CapBig * (sizeof(double2) + sizeof(uint32_t));
+        int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)nl, freeb / 4 / per_row));
+        if (const char *rc_env = std::getenv("VO_ENVELOPE_ROW_CHUNK")) {  // tests: smaller chunks
+          const int v = std::atoi(rc_env);
+          if (v > 0) chunk = std::min(chunk, v);
+        }
+        rc = dalloc(ctx, &gz2, (size_t)2 * kE2CapBig * chunk);
+        if (!rc) rc = dalloc(ctx, &gk2, (size_t)2 * kE2CapBig * chunk);
+        for (int r0 = 0; !rc && r0 < nl && !hflags[kFlagFatal]; r0 += chunk) {
+          const int cnt = std::min(chunk, nl - r0);
+          E2Args ab = a2;
+          ab.gz = gz2;
+          ab.gk = gk2;
+          ab.list = list + r0;
+          k_env2<true><<<cnt, kE2Threads, e2_smem_bytes(true), ctx->stream>>>(ab, cnt);
           ctx->launches += 1;
           rc = flags_now();
         }
