@@ -537,7 +537,6 @@ __global__ void __launch_bounds__(kE2Threads, BIG ? 5 : 1) k_env2(E2Args A, int 
   __shared__ BlockScratch bs;
   __shared__ double2 U[kE2Out], U1[kE2Out], Mrg[2 * kE2Out];
   __shared__ int s_hist[2 * kE2Stage + 2];
-  __shared__ int s_abort, s_nu;
   const int tid = threadIdx.x;
   const int cap = BIG ? kE2CapBig : A.cap_small;
   // shared layout: staging (2 buffers), then (first launch) stadiums S and T
@@ -568,7 +567,6 @@ __global__ void __launch_bounds__(kE2Threads, BIG ? 5 : 1) k_env2(E2Args A, int 
   if (tid == 0) {
     mbar_init(&bar[0]);
     mbar_init(&bar[1]);
-    s_abort = 0;
   }
   __syncthreads();
   uint32_t phase[2] = {0u, 0u};

@@ -46,7 +46,6 @@
 namespace vo {
 namespace {
 
-constexpr int kKA = kUnionCap;     // union capacity of the main kernels
 constexpr int kKM = kUnionCapMid;  // union capacity of the second tier
 // Block shape of k_fast: one warp (one patch of columns), at most 64
 // registers so that 32 warps fit an SM; measured faster than four-warp blocks
