@@ -17,7 +17,8 @@ pairs) is larger than L2 (129 MB), so no flush is needed between steps.
           "plain vs batched+learned" comparison.
   e2e   : the same metric through the C ABI from pinned host buffers: upload,
           vo_morph_batched (plan, replay, outputs) and download of the result
-          inside the timed region.
+          inside the timed region, the copies on the context's copy stream so
+          that they overlap the neighbouring steps' dilations.
   cpu_baseline : the reference's own `ours` (oracle/_ref, multithreaded) or,
           where the reference could not be built, the oracle restatement, timed
           on a bounded slab of the same workload (rank 0, N=1).
@@ -543,41 +544,53 @@ def main():
     out_offs = torch.empty(ncols + 1, dtype=torch.int32, pin_memory=True).numpy()
     out_z = torch.empty(max(2 * out_segs, 2), dtype=torch.float64, pin_memory=True).numpy()
 
-    # host-clock split of a step: the upload call (asynchronous copies, offsets checked while they
-    # run), the morphology call (its own total_ms: plan, replay, outputs; it waits for the upload),
-    # the download (synchronous) and the frees
-    parts = {"upload_ms": 0.0, "morph_ms": 0.0, "morph_call_ms": 0.0, "download_ms": 0.0, "free_ms": 0.0}
+    # Steps are pipelined through the copy stream of the context: the upload of step i + 1 is queued
+    # (vo_volume_upload_async) before the dilation of step i and the download of step i
+    # (vo_volume_download_async) after it, so both copies overlap a dilation; every step still moves
+    # its input in and its result out inside the timed region, which ends when the last download has
+    # landed (vo_sync). Host-clock split per step: the upload call (offsets checked while the copy
+    # runs), the morphology call and its own total_ms (plan, replay, outputs), the download call and
+    # the frees; `drain_ms` is the final wait for the last download.
+    parts = {"upload_ms": 0.0, "morph_ms": 0.0, "morph_call_ms": 0.0, "download_ms": 0.0, "free_ms": 0.0,
+             "drain_ms": 0.0}
+    pin_zv = pin_z[:z.size]
 
-    def e2e_step():
-        t0 = time.perf_counter()
-        v = ctx.upload(grid, pin_offs, pin_z[:z.size])
-        t1 = time.perf_counter()
-        if args.method == "batched":
-            outs, tm = ctx.morph_batched([v], ["dilation"], [args.radius], "fast")
-            o = outs[0]
-        else:
-            o, tm = ctx.morph(v, "dilation", args.radius, args.method)
-        t2 = time.perf_counter()
-        n_o, n_z = ctx.download_into(o, out_offs, out_z)
-        t3 = time.perf_counter()
-        o.free()
-        v.free()
-        t4 = time.perf_counter()
-        for k, dt in (("upload_ms", t1 - t0), ("morph_call_ms", t2 - t1), ("download_ms", t3 - t2),
-                      ("free_ms", t4 - t3)):
-            parts[k] += dt * 1e3
-        parts["morph_ms"] += tm["total_ms"]
-        return 4 * n_o + 8 * n_z
+    def e2e_run(steps):
+        d2h = 0
+        nxt = ctx.upload_async(grid, pin_offs, pin_zv)
+        for i in range(steps):
+            t0 = time.perf_counter()
+            cur = nxt
+            if i + 1 < steps:
+                nxt = ctx.upload_async(grid, pin_offs, pin_zv)
+            t1 = time.perf_counter()
+            if args.method == "batched":
+                outs, tm = ctx.morph_batched([cur], ["dilation"], [args.radius], "fast")
+                o = outs[0]
+            else:
+                o, tm = ctx.morph(cur, "dilation", args.radius, args.method)
+            t2 = time.perf_counter()
+            n_o, n_z = ctx.download_async(o, out_offs, out_z)
+            t3 = time.perf_counter()
+            o.free()
+            cur.free()
+            t4 = time.perf_counter()
+            for k, dt in (("upload_ms", t1 - t0), ("morph_call_ms", t2 - t1), ("download_ms", t3 - t2),
+                          ("free_ms", t4 - t3)):
+                parts[k] += dt * 1e3
+            parts["morph_ms"] += tm["total_ms"]
+            d2h = 4 * n_o + 8 * n_z
+        t5 = time.perf_counter()
+        ctx.sync()
+        parts["drain_ms"] += (time.perf_counter() - t5) * 1e3
+        return d2h
 
-    for _ in range(max(1, args.warmup)):
-        e2e_step()
+    e2e_run(max(1, args.warmup))
     barrier()
     parts.update({k: 0.0 for k in parts})
     clocks.start()
     t0 = time.perf_counter()
-    d2h = 0
-    for _ in range(args.steps):
-        d2h = e2e_step()
+    d2h = e2e_run(args.steps)
     barrier()
     e2e_s = maxreduce(time.perf_counter() - t0)
     e2e_clk = clocks.stop()

@@ -108,7 +108,7 @@ const char *vo_last_error(const vo_ctx *ctx);
 /* The context's cudaStream_t, as void*, so a host can order its own work or
  * record events on it. */
 void *vo_stream(vo_ctx *ctx);
-/* Blocks until the context's stream is idle. */
+/* Blocks until the context's streams (compute and copy) are idle. */
 int vo_sync(vo_ctx *ctx);
 
 /* Volumes. Upload copies host CSR into a new device volume
@@ -118,6 +118,19 @@ int vo_sync(vo_ctx *ctx);
  * that returns results (vo_morph, vo_volume_download, ...) has returned. */
 int vo_volume_upload(vo_ctx *ctx, const vo_grid *grid, const int32_t *offs, const double *z,
                      vo_volume **out);
+/* Asynchronous copies on the context's second (copy) stream, so that they
+ * overlap the kernels of its compute stream (no reference counterpart).
+ * vo_volume_upload_async: as vo_volume_upload (same checks, returns before the
+ *   copy ends); the host buffers must be page-locked and stay unchanged until
+ *   vo_sync, or a call that returns results, has returned. Every entry point
+ *   that reads the volume orders its device work after the copy.
+ * vo_volume_download_async: copies the volume into page-locked host buffers
+ *   once the work already queued on the compute stream has produced it, and
+ *   returns; the buffers hold the result after vo_sync. Freeing the volume
+ *   waits for the copy in stream order. */
+int vo_volume_upload_async(vo_ctx *ctx, const vo_grid *grid, const int32_t *offs, const double *z,
+                           vo_volume **out);
+int vo_volume_download_async(vo_ctx *ctx, const vo_volume *v, int32_t *offs, double *z);
 /* Grid and segment count of a volume (the size query before a download). */
 int vo_volume_info(vo_ctx *ctx, const vo_volume *v, vo_grid *grid, int64_t *nseg);
 /* Copies a volume to caller-allocated host buffers: offs[nx*ny+1], z[2*nseg]. */

@@ -102,8 +102,11 @@ SIGNATURES = {
     "vo_sync": (C.c_int, [_P]),
     "vo_volume_upload": (C.c_int, [_P, C.POINTER(_Grid), C.POINTER(C.c_int32), C.POINTER(C.c_double),
                                    C.POINTER(_P)]),
+    "vo_volume_upload_async": (C.c_int, [_P, C.POINTER(_Grid), C.POINTER(C.c_int32), C.POINTER(C.c_double),
+                                   C.POINTER(_P)]),
     "vo_volume_info": (C.c_int, [_P, _P, C.POINTER(_Grid), C.POINTER(C.c_int64)]),
     "vo_volume_download": (C.c_int, [_P, _P, C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
+    "vo_volume_download_async": (C.c_int, [_P, _P, C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
     "vo_volume_device_ptrs": (C.c_int, [_P, _P, C.POINTER(_P), C.POINTER(_P)]),
     "vo_volume_free": (None, [_P, _P]),
     "vo_morph": (C.c_int, [_P, C.c_int, C.c_int, C.c_double, _P, C.POINTER(_P), C.POINTER(_Timings)]),
@@ -273,6 +276,30 @@ class Context:
         self._check(lib().vo_volume_upload(self.handle, C.byref(g), _i32p(offs), _f64p(zz), C.byref(h)),
                     "vo_volume_upload")
         return Volume(self, h.value)
+
+    def upload_async(self, grid: Grid, offs, z) -> Volume:
+        """vo_volume_upload_async: the copy runs on the context's copy stream. offs and z must be
+        page-locked (e.g. numpy views of pinned torch tensors), contiguous, and kept unchanged (and
+        alive) until sync() or a call that returns results."""
+        if offs.dtype != np.int32 or z.dtype != np.float64 or not offs.flags.c_contiguous or \
+                not z.flags.c_contiguous:
+            raise ValueError("upload_async needs contiguous int32 offsets and float64 pairs")
+        if offs.size != grid.ncols + 1:
+            raise ValueError("offs must have nx*ny+1 entries")
+        h = C.c_void_p()
+        g = grid.to_c()
+        self._check(lib().vo_volume_upload_async(self.handle, C.byref(g), _i32p(offs), _f64p(z), C.byref(h)),
+                    "vo_volume_upload_async")
+        return Volume(self, h.value)
+
+    def download_async(self, v: Volume, offs_buf, z_buf):
+        """vo_volume_download_async into page-locked caller buffers; they hold the volume after
+        sync(). Returns the (offsets, values) counts that will be written."""
+        if offs_buf.size < v.grid.ncols + 1 or z_buf.size < 2 * v.nseg:
+            raise ValueError("download buffers too small")
+        self._check(lib().vo_volume_download_async(self.handle, v.handle, _i32p(offs_buf), _f64p(z_buf)),
+                    "vo_volume_download_async")
+        return v.grid.ncols + 1, 2 * v.nseg
 
     def download(self, v: Volume):
         offs = np.empty(v.grid.ncols + 1, dtype=np.int32)

@@ -174,6 +174,10 @@ int get_tables(vo_ctx *ctx, double R, int kmax, const DeviceTables **out) {
   return VO_OK;
 }
 
+void vol_wait(vo_ctx *ctx, const vo_volume *v) {
+  if (ctx && v && v->ready) cudaStreamWaitEvent(ctx->stream, v->ready, 0);
+}
+
 int volume_alloc(vo_ctx *ctx, const vo_grid &g, int64_t nseg, vo_volume **out) {
   vo_volume *v = new (std::nothrow) vo_volume();
   if (!v) return set_error(ctx, VO_ENOMEM, "host allocation");
@@ -222,7 +226,11 @@ int vo_create(vo_ctx **out, int device) {
   if (!ctx) return VO_ENOMEM;
   ctx->device = device;
   if (cudaSetDevice(device) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->ev_order, cudaEventDisableTiming) != cudaSuccess) {
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     delete ctx;
     return VO_ECUDA;
   }
@@ -246,6 +254,7 @@ int vo_create(vo_ctx **out, int device) {
 void vo_destroy(vo_ctx *ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
+  if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (DeviceTables *d : ctx->tables) {
     cudaFree(d->H);
@@ -260,6 +269,8 @@ void vo_destroy(vo_ctx *ctx) {
   cudaFree(ctx->d_flags);
   cudaFree(ctx->d_total);
   if (ctx->h_total) cudaFreeHost(ctx->h_total);
+  if (ctx->ev_order) cudaEventDestroy(ctx->ev_order);
+  if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -270,6 +281,7 @@ void *vo_stream(vo_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
 
 int vo_sync(vo_ctx *ctx) {
   if (!ctx) return VO_EINVAL;
+  VO_CK(ctx, cudaStreamSynchronize(ctx->copy_stream));
   VO_CK(ctx, cudaStreamSynchronize(ctx->stream));
   return VO_OK;
 }
@@ -305,6 +317,40 @@ int vo_volume_upload(vo_ctx *ctx, const vo_grid *grid, const int32_t *offs, cons
   return VO_OK;
 }
 
+int vo_volume_upload_async(vo_ctx *ctx, const vo_grid *grid, const int32_t *offs, const double *z,
+                           vo_volume **out) {
+  if (!ctx || !out || !offs || !grid_ok(grid)) return set_error(ctx, VO_EINVAL, "upload: bad grid");
+  *out = nullptr;
+  const int64_t ncols = (int64_t)grid->nx * grid->ny;
+  if (offs[0] != 0) return set_error(ctx, VO_EINVAL, "upload: offs[0] must be 0");
+  const int64_t nseg = offs[ncols];
+  if (nseg < 0) return set_error(ctx, VO_EINVAL, "upload: offsets must not decrease");
+  if (nseg > 0 && !z) return set_error(ctx, VO_EINVAL, "upload: z is NULL");
+  cudaSetDevice(ctx->device);
+  vo_volume *v = nullptr;
+  int rc = volume_alloc(ctx, *grid, nseg, &v);
+  if (rc) return rc;
+  // the memory is allocated in the context's stream order: the copy stream starts after that
+  cudaError_t e = cudaEventCreateWithFlags(&v->ready, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_order, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_order, 0);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(v->offs, offs, sizeof(int32_t) * (ncols + 1), cudaMemcpyHostToDevice, ctx->copy_stream);
+  if (e == cudaSuccess && nseg > 0)
+    e = cudaMemcpyAsync(v->z, z, sizeof(double) * 2 * nseg, cudaMemcpyHostToDevice, ctx->copy_stream);
+  if (e == cudaSuccess) e = cudaEventRecord(v->ready, ctx->copy_stream);
+  bool monotone = true;
+  for (int64_t c = 0; c < ncols; ++c) monotone &= offs[c + 1] >= offs[c];
+  if (e != cudaSuccess || !monotone) {
+    cudaStreamSynchronize(ctx->copy_stream);
+    vo_volume_free(ctx, v);
+    if (e != cudaSuccess) return cuda_error(ctx, e, "upload_async");
+    return set_error(ctx, VO_EINVAL, "upload: offsets must not decrease");
+  }
+  *out = v;
+  return VO_OK;
+}
+
 int vo_volume_info(vo_ctx *ctx, const vo_volume *v, vo_grid *grid, int64_t *nseg) {
   if (!ctx || !v) return VO_EINVAL;
   if (grid) *grid = v->grid;
@@ -315,6 +361,7 @@ int vo_volume_info(vo_ctx *ctx, const vo_volume *v, vo_grid *grid, int64_t *nseg
 int vo_volume_download(vo_ctx *ctx, const vo_volume *v, int32_t *offs, double *z) {
   if (!ctx || !v || !offs || (v->nseg > 0 && !z)) return set_error(ctx, VO_EINVAL, "download: NULL buffer");
   cudaSetDevice(ctx->device);
+  vol_wait(ctx, v);
   const int64_t ncols = (int64_t)v->grid.nx * v->grid.ny;
   VO_CK(ctx, cudaMemcpyAsync(offs, v->offs, sizeof(int32_t) * (ncols + 1), cudaMemcpyDeviceToHost,
                              ctx->stream));
@@ -325,8 +372,27 @@ int vo_volume_download(vo_ctx *ctx, const vo_volume *v, int32_t *offs, double *z
   return VO_OK;
 }
 
+int vo_volume_download_async(vo_ctx *ctx, const vo_volume *v, int32_t *offs, double *z) {
+  if (!ctx || !v || !offs || (v->nseg > 0 && !z)) return set_error(ctx, VO_EINVAL, "download: NULL buffer");
+  cudaSetDevice(ctx->device);
+  vol_wait(ctx, v);
+  if (!v->copied) VO_CK(ctx, cudaEventCreateWithFlags(&v->copied, cudaEventDisableTiming));
+  // the copies start once the context's stream has produced the volume
+  VO_CK(ctx, cudaEventRecord(ctx->ev_order, ctx->stream));
+  VO_CK(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_order, 0));
+  const int64_t ncols = (int64_t)v->grid.nx * v->grid.ny;
+  VO_CK(ctx, cudaMemcpyAsync(offs, v->offs, sizeof(int32_t) * (ncols + 1), cudaMemcpyDeviceToHost,
+                             ctx->copy_stream));
+  if (v->nseg > 0)
+    VO_CK(ctx, cudaMemcpyAsync(z, v->z, sizeof(double) * 2 * v->nseg, cudaMemcpyDeviceToHost,
+                               ctx->copy_stream));
+  VO_CK(ctx, cudaEventRecord(v->copied, ctx->copy_stream));
+  return VO_OK;
+}
+
 int vo_volume_device_ptrs(vo_ctx *ctx, const vo_volume *v, void **offs, void **z) {
   if (!ctx || !v) return VO_EINVAL;
+  if (v->ready) cudaEventSynchronize(v->ready);  // the caller's own work may use another stream
   if (offs) *offs = v->offs;
   if (z) *z = v->z;
   return VO_OK;
@@ -334,10 +400,24 @@ int vo_volume_device_ptrs(vo_ctx *ctx, const vo_volume *v, void **offs, void **z
 
 void vo_volume_free(vo_ctx *ctx, vo_volume *v) {
   if (!ctx || !v) return;
-  if (v->owns) {
-    dfree(ctx, v->offs);
-    dfree(ctx, v->z);
+  if (v->copied) {
+    // downloaded asynchronously: freed in the copy stream's order, after the download and after the
+    // work queued so far on the compute stream, which then need not wait for the download
+    cudaEventRecord(ctx->ev_order, ctx->stream);
+    cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_order, 0);
+    if (v->owns) {
+      if (v->offs) cudaFreeAsync(v->offs, ctx->copy_stream);
+      if (v->z) cudaFreeAsync(v->z, ctx->copy_stream);
+    }
+  } else {
+    if (v->ready) cudaStreamWaitEvent(ctx->stream, v->ready, 0);  // after its upload
+    if (v->owns) {
+      dfree(ctx, v->offs);
+      dfree(ctx, v->z);
+    }
   }
+  if (v->ready) cudaEventDestroy(v->ready);
+  if (v->copied) cudaEventDestroy(v->copied);
   delete v;
 }
 
@@ -351,6 +431,7 @@ int vo_morph(vo_ctx *ctx, int op, int method, double radius, const vo_volume *in
     return set_error(ctx, VO_EINVAL, "morph: unknown method");
   if (!(radius >= 0) || radius > 255) return set_error(ctx, VO_EINVAL, "morph: radius must be in [0, 255]");
   cudaSetDevice(ctx->device);
+  vol_wait(ctx, in);
   *out = nullptr;
   ctx->err.clear();
   ctx->launches = 0;
@@ -405,6 +486,7 @@ int vo_morph_batched(vo_ctx *ctx, int n, const int *ops, const double *radii, in
         return set_error(ctx, VO_EINVAL, "morph_batched: bad volume, op or radius");
     }
     cudaSetDevice(ctx->device);
+    for (int i = 0; i < n; ++i) vol_wait(ctx, ins[i]);
     ctx->err.clear();
     ctx->launches = 0;
     return morph_batched_fast(ctx, n, ops, radii, ins, outs, tm);

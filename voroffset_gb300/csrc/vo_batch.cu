@@ -693,6 +693,7 @@ int vo_batch_create(vo_ctx *ctx, int n, const int *ops, const double *radii, int
   if (!valid_batch(n, ops, radii, method, ins))
     return set_error(ctx, VO_EINVAL, "batch: bad volume, op, radius or method (VO_METHOD_FAST only)");
   cudaSetDevice(ctx->device);
+  for (int i = 0; i < n; ++i) vol_wait(ctx, ins[i]);  // before any capture: the plan then reads them in order
   ctx->err.clear();
   const auto t0 = std::chrono::steady_clock::now();
   vo_batch *b = new vo_batch();

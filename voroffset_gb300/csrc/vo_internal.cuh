@@ -93,11 +93,17 @@ struct vo_volume {
   int32_t *offs = nullptr;  // device [nx*ny+1]
   double2 *z = nullptr;     // device [nseg]
   bool owns = true;
+  // Copies on the context's copy stream (vo_volume_upload_async /
+  // vo_volume_download_async): `ready` completes when the upload has landed,
+  // `copied` when the last download has left; null when none was made.
+  mutable cudaEvent_t ready = nullptr, copied = nullptr;
 };
 
 struct vo_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t copy_stream = nullptr;  // asynchronous uploads and downloads
+  cudaEvent_t ev_order = nullptr;      // orders the copy stream after the compute stream
   std::string err;
   std::vector<vo::DeviceTables *> tables;  // small cache keyed by (R, kmax)
   cudaEvent_t ev[8] = {};
@@ -113,6 +119,10 @@ struct vo_ctx {
 };
 
 namespace vo {
+
+// Orders the context's stream after the asynchronous upload of v, if any (every
+// entry point that reads a volume calls it first).
+void vol_wait(vo_ctx *ctx, const vo_volume *v);
 
 // Error helpers: set ctx->err and return a status.
 int set_error(vo_ctx *ctx, int code, const std::string &msg);

@@ -114,6 +114,7 @@ extern "C" int vo_volume_measure(vo_ctx *ctx, const vo_volume *v, int64_t *num_s
   if (!ctx) return VO_EINVAL;
   if (!v || !num_segments || !volume) return set_error(ctx, VO_EINVAL, "measure: NULL argument");
   cudaSetDevice(ctx->device);
+  vol_wait(ctx, v);
   ctx->err.clear();
   const int ncols = v->grid.nx * v->grid.ny;
   const int nblk = std::max(1, (ncols + kThreads - 1) / kThreads);
@@ -150,6 +151,8 @@ extern "C" int vo_xor_volume(vo_ctx *ctx, const vo_volume *a, const vo_volume *b
   if (a->grid.nx != b->grid.nx || a->grid.ny != b->grid.ny)
     return set_error(ctx, VO_EINVAL, "xor: grids differ");
   cudaSetDevice(ctx->device);
+  vol_wait(ctx, a);
+  vol_wait(ctx, b);
   const int ncols = a->grid.nx * a->grid.ny;
   const int nblk = (ncols + kThreads - 1) / kThreads;
   double *partial = nullptr, *d_out = nullptr;

@@ -468,6 +468,7 @@ int vo_sizer_get_params(vo_ctx *ctx, const vo_sizer *s, float *params, int count
 
 int vo_sizer_tile_features(vo_ctx *ctx, const vo_volume *v, double radius, float *feats, int *ntiles) {
   if (!ctx || !v || !ntiles) return VO_EINVAL;
+  vol_wait(ctx, v);
   const int tx = (v->grid.nx + kTile - 1) / kTile, ty = (v->grid.ny + kTile - 1) / kTile;
   if (!feats) {
     *ntiles = tx * ty;
@@ -490,6 +491,8 @@ int vo_sizer_tile_targets(vo_ctx *ctx, const vo_volume *in, const vo_volume *res
                           int *ntiles) {
   if (!ctx || !in || !result || !targets || !ntiles) return VO_EINVAL;
   if (in->grid.nx != result->grid.nx || in->grid.ny != result->grid.ny) return VO_EINVAL;
+  vol_wait(ctx, in);
+  vol_wait(ctx, result);
   const int nx = in->grid.nx, ny = in->grid.ny;
   const int tx = (nx + kTile - 1) / kTile, ty = (ny + kTile - 1) / kTile;
   const DeviceTables *T = nullptr;
