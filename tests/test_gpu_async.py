@@ -108,3 +108,23 @@ def test_async_inputs_to_plans_and_reductions(ctx, vo):
         v.free()
     ctx.sync()
     del to, tz
+
+
+@pytest.mark.parametrize("where", [5, 700_000, 1_099_998])
+def test_uploads_reject_decreasing_offsets_on_large_grids(ctx, vo, where):
+    """Grids of more than 2^20 columns are checked by several host threads: a
+    decrease anywhere (first, middle or last chunk) is refused by both uploads."""
+    g = vo.Grid(1100, 1000, (0, 0, 0), (1100, 1000, 10), 1.0, 0)
+    offs = np.arange(g.ncols + 1, dtype=np.int32) // 4
+    z = np.tile(np.array([1.0, 2.0]), int(offs[-1]))
+    to, po = pinned(offs, np.int32)
+    tz, pz = pinned(z, np.float64)
+    good = ctx.upload_async(g, po, pz)
+    good.free()
+    po[where] = po[where + 1] + 1
+    with pytest.raises(vo.GpuError):
+        ctx.upload(g, np.array(po), z)
+    with pytest.raises(vo.GpuError):
+        ctx.upload_async(g, po, pz)
+    ctx.sync()
+    del to, tz

@@ -8,6 +8,8 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <thread>
+#include <vector>
 
 #include "vo_internal.cuh"
 
@@ -201,6 +203,29 @@ using namespace vo;
 
 namespace {
 
+// Whether offs[0..ncols] never decreases; large arrays are checked by a few
+// host threads at once (the check runs while the upload's copies do).
+bool offsets_monotone(const int32_t *offs, int64_t ncols) {
+  auto scan = [offs](int64_t c0, int64_t c1) {
+    int bad = 0;
+    for (int64_t c = c0; c < c1; ++c) bad |= offs[c + 1] < offs[c];
+    return bad == 0;
+  };
+  const unsigned hw = std::thread::hardware_concurrency();
+  const int nt = ncols < (1 << 20) || hw < 2 ? 1 : (int)std::min(8u, hw);
+  if (nt == 1) return scan(0, ncols);
+  std::vector<char> ok(nt, 1);
+  std::vector<std::thread> th;
+  const int64_t per = (ncols + nt - 1) / nt;
+  for (int t = 1; t < nt; ++t)
+    th.emplace_back([&, t] { ok[t] = scan(std::min(ncols, t * per), std::min(ncols, (t + 1) * per)); });
+  ok[0] = scan(0, std::min(ncols, per));
+  for (std::thread &x : th) x.join();
+  for (char v : ok)
+    if (!v) return false;
+  return true;
+}
+
 bool grid_ok(const vo_grid *g) {
   return g && g->nx > 0 && g->ny > 0 && (int64_t)g->nx * g->ny < (1ll << 31) - 1 &&
          g->spacing > 0 && std::isfinite(g->spacing);
@@ -305,8 +330,7 @@ int vo_volume_upload(vo_ctx *ctx, const vo_grid *grid, const int32_t *offs, cons
                                   cudaMemcpyHostToDevice, ctx->stream);
   if (e == cudaSuccess && nseg > 0)
     e = cudaMemcpyAsync(v->z, z, sizeof(double) * 2 * nseg, cudaMemcpyHostToDevice, ctx->stream);
-  bool monotone = true;
-  for (int64_t c = 0; c < ncols; ++c) monotone &= offs[c + 1] >= offs[c];
+  const bool monotone = offsets_monotone(offs, ncols);
   if (e != cudaSuccess || !monotone) {
     cudaStreamSynchronize(ctx->stream);
     vo_volume_free(ctx, v);
@@ -339,8 +363,7 @@ int vo_volume_upload_async(vo_ctx *ctx, const vo_grid *grid, const int32_t *offs
   if (e == cudaSuccess && nseg > 0)
     e = cudaMemcpyAsync(v->z, z, sizeof(double) * 2 * nseg, cudaMemcpyHostToDevice, ctx->copy_stream);
   if (e == cudaSuccess) e = cudaEventRecord(v->ready, ctx->copy_stream);
-  bool monotone = true;
-  for (int64_t c = 0; c < ncols; ++c) monotone &= offs[c + 1] >= offs[c];
+  const bool monotone = offsets_monotone(offs, ncols);
   if (e != cudaSuccess || !monotone) {
     cudaStreamSynchronize(ctx->copy_stream);
     vo_volume_free(ctx, v);
