@@ -226,6 +226,8 @@ bool offsets_monotone(const int32_t *offs, int64_t ncols) {
   return true;
 }
 
+constexpr int64_t kCopyPiece = (64ll << 20) / 16;  // segments per asynchronous copy piece (64 MB)
+
 bool grid_ok(const vo_grid *g) {
   return g && g->nx > 0 && g->ny > 0 && (int64_t)g->nx * g->ny < (1ll << 31) - 1 &&
          g->spacing > 0 && std::isfinite(g->spacing);
@@ -360,8 +362,11 @@ int vo_volume_upload_async(vo_ctx *ctx, const vo_grid *grid, const int32_t *offs
   if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_order, 0);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(v->offs, offs, sizeof(int32_t) * (ncols + 1), cudaMemcpyHostToDevice, ctx->copy_stream);
-  if (e == cudaSuccess && nseg > 0)
-    e = cudaMemcpyAsync(v->z, z, sizeof(double) * 2 * nseg, cudaMemcpyHostToDevice, ctx->copy_stream);
+  // in pieces of 64 MB, so that small copies of the compute stream can be scheduled between them
+  // rather than behind one long transfer
+  for (int64_t k = 0; e == cudaSuccess && k < nseg; k += kCopyPiece)
+    e = cudaMemcpyAsync(v->z + k, z + 2 * k, sizeof(double) * 2 * std::min<int64_t>(kCopyPiece, nseg - k),
+                        cudaMemcpyHostToDevice, ctx->copy_stream);
   if (e == cudaSuccess) e = cudaEventRecord(v->ready, ctx->copy_stream);
   const bool monotone = offsets_monotone(offs, ncols);
   if (e != cudaSuccess || !monotone) {
@@ -406,9 +411,9 @@ int vo_volume_download_async(vo_ctx *ctx, const vo_volume *v, int32_t *offs, dou
   const int64_t ncols = (int64_t)v->grid.nx * v->grid.ny;
   VO_CK(ctx, cudaMemcpyAsync(offs, v->offs, sizeof(int32_t) * (ncols + 1), cudaMemcpyDeviceToHost,
                              ctx->copy_stream));
-  if (v->nseg > 0)
-    VO_CK(ctx, cudaMemcpyAsync(z, v->z, sizeof(double) * 2 * v->nseg, cudaMemcpyDeviceToHost,
-                               ctx->copy_stream));
+  for (int64_t k = 0; k < v->nseg; k += kCopyPiece)
+    VO_CK(ctx, cudaMemcpyAsync(z + 2 * k, v->z + k, sizeof(double) * 2 * std::min<int64_t>(kCopyPiece, v->nseg - k),
+                               cudaMemcpyDeviceToHost, ctx->copy_stream));
   VO_CK(ctx, cudaEventRecord(v->copied, ctx->copy_stream));
   return VO_OK;
 }
