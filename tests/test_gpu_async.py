@@ -128,3 +128,31 @@ def test_uploads_reject_decreasing_offsets_on_large_grids(ctx, vo, where):
         ctx.upload_async(g, po, pz)
     ctx.sync()
     del to, tz
+
+
+def test_async_round_trip_in_pieces(ctx, vo):
+    """More segments than one 64 MB copy piece (4,194,304): uploaded and
+    downloaded asynchronously in several pieces, the volume comes back bit for
+    bit, and a dilation of it equals the synchronous path's."""
+    g = vo.Grid(2048, 1024, (0, 0, 0), (2048, 1024, 64), 1.0, 0)
+    rng = np.random.default_rng(5)
+    offs = (np.arange(g.ncols + 1, dtype=np.int64) * 3).astype(np.int32)  # 6.3 M segments
+    base = np.sort(rng.uniform(0.0, 60.0, (g.ncols, 6)), axis=1)
+    z = np.ascontiguousarray(base.reshape(-1))
+    to, po = pinned(offs, np.int32)
+    tz, pz = pinned(z, np.float64)
+    v = ctx.upload_async(g, po, pz)
+    tb1, ho = pinned(np.zeros(g.ncols + 1, np.int32), np.int32)
+    tb2, hz = pinned(np.zeros(z.size, np.float64), np.float64)
+    ctx.download_async(v, ho, hz)
+    ctx.sync()
+    assert np.array_equal(ho, offs) and np.array_equal(hz, z)
+    out, _ = ctx.morph(v, "dilation", 2.0, "fast")
+    ta, ro = pinned(np.zeros(g.ncols + 1, np.int32), np.int32)
+    tb, rz = pinned(np.zeros(2 * out.nseg, np.float64), np.float64)
+    n_o, n_z = ctx.download_async(out, ro, rz)
+    ctx.sync()
+    ref_o, ref_z = ctx.download(out)
+    assert np.array_equal(ro[:n_o], ref_o) and np.array_equal(rz[:n_z], ref_z)
+    out.free()
+    v.free()
