@@ -6,7 +6,9 @@
   reference sources exist;
 * plus the properties the reference's own cross-checks give: the two methods
   agree (`ours` vs `brute_force`, offset3d.cpp:47,105-112), a dilation
-  contains its input, an erosion is inside it, radius 0 is the identity union.
+  contains its input, an erosion is inside it, opening is inside the input
+  and closing around it, a larger radius dilates further, radius 0 is the
+  identity union.
 """
 from __future__ import annotations
 
@@ -89,6 +91,62 @@ def test_dilation_contains_input_erosion_inside(oracle, vo):
             assert _covered(do, dz, c, a, b)
         for a, b in ez[2 * eo[c]:2 * eo[c + 1]].reshape(-1, 2):
             assert _covered(offs, z, c, a, b)
+
+
+def _covered_eps(offs, z, c, lo, hi, eps):
+    s = z[2 * offs[c]:2 * offs[c + 1]].reshape(-1, 2)
+    return bool(np.any((s[:, 0] - eps <= lo) & (hi <= s[:, 1] + eps)))
+
+
+def _inside(ao, az, bo, bz, eps=0.0):
+    """Every interval of volume A lies in one interval of volume B (same grid),
+    up to eps at either end."""
+    for c in range(len(ao) - 1):
+        s = bz[2 * bo[c]:2 * bo[c + 1]].reshape(-1, 2)
+        for a, b in az[2 * ao[c]:2 * ao[c + 1]].reshape(-1, 2):
+            if not np.any((s[:, 0] - eps <= a) & (b <= s[:, 1] + eps)):
+                return False
+    return True
+
+
+@pytest.mark.parametrize("r", [2.5, 6.0])
+def test_opening_inside_input_inside_closing(oracle, vo, r):
+    """Opening is anti-extensive and closing extensive (the structuring element
+    holds its centre), as the reference's chains of offset3d.cpp:124-133 give,
+    up to the rounding of an endpoint moved down by H and up again (a few ulps:
+    at most 5.3e-15 here). Closing is extensive only away from the volume's
+    border: its erosion takes everything outside the grid and outside the z
+    range as empty (Voronoi.cpp:8-89), so within r of them it erodes material
+    the dilation could not restore."""
+    grid, offs, z = vo.synth_volume(vo.SynthSpec(40, ny=36, n_spheres=18, s_rmin=2, s_rmax=10, n_cyl=3, seed=21))
+    g = ogrid(oracle, grid)
+    oo, oz = oracle.morph(g, offs, z, r, "opening")
+    co, cz = oracle.morph(g, offs, z, r, "closing")
+    assert _inside(oo, oz, offs, z, eps=1e-12)
+    m = int(np.ceil(r)) + 1
+    zmax = grid.extent[2]
+    checked = 0
+    for c in range(grid.ncols):
+        x, y = c % grid.nx, c // grid.nx
+        if not (m <= x < grid.nx - m and m <= y < grid.ny - m):
+            continue
+        for a, b in z[2 * offs[c]:2 * offs[c + 1]].reshape(-1, 2):
+            if a > r + 1 and b < zmax - r - 1:
+                assert _covered_eps(co, cz, c, a, b, 1e-12), (c, a, b)
+                checked += 1
+    assert checked > 50
+
+
+def test_dilation_grows_with_radius(oracle, vo):
+    """A larger ball holds the smaller one, so its dilation holds the other's."""
+    grid, offs, z = vo.synth_volume(vo.SynthSpec(40, ny=32, n_spheres=15, s_rmin=2, s_rmax=9, n_cyl=2, seed=22))
+    g = ogrid(oracle, grid)
+    prev = None
+    for r in (1.0, 2.5, 4.0, 7.25):
+        cur = oracle.morph(g, offs, z, r, "dilation")
+        if prev is not None:
+            assert _inside(prev[0], prev[1], cur[0], cur[1]), r
+        prev = cur
 
 
 def test_radius_zero_is_identity(oracle, vo):
