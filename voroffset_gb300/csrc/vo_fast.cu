@@ -358,8 +358,15 @@ __global__ void __launch_bounds__(kFB *kFBY, 1024 / (kFB * kFBY)) k_fast(FastArg
                                                     int *ovf_count, int *ovf_cols) {
   extern __shared__ float2 sv_dyn[];
   const int tid = threadIdx.x + kFB * threadIdx.y;
-  const int x = blockIdx.x * kPatchX + threadIdx.x % kPatchX;
-  const int y = blockIdx.y * kPatchY + threadIdx.x / kPatchX;
+  // blocks (patches) in bands of 512 columns, all rows of a band before the next: the blocks running
+  // together cover a compact region, whose source columns stay in L2
+  constexpr int kBand = 512 / kPatchX;
+  const int tiles_x = (A.nx + kPatchX - 1) / kPatchX, tiles_y = (A.ny + kPatchY - 1) / kPatchY;
+  const int band = (int)blockIdx.x / (kBand * tiles_y);
+  const int rb = (int)blockIdx.x - band * kBand * tiles_y;
+  const int bw = min(kBand, tiles_x - band * kBand);
+  const int x = (band * kBand + rb % bw) * kPatchX + threadIdx.x % kPatchX;
+  const int y = (rb / bw) * kPatchY + threadIdx.x / kPatchX;
   if (x >= A.nx || y >= A.ny) return;
   const int c = x + A.nx * y;
   const float E = *A.E;
@@ -851,7 +858,7 @@ int dilate_fast(vo_ctx *ctx, double R, const vo_volume *in, vo_volume **out, vo_
   }
   FastArgs A{nx, ny, h.W, in->offs, in->offs + 1, (const double *)in->z, zf, T->Hf, T->H, dpairs,
              (int)pairs.size(), dE, col, prec, dmask, mbits};
-  const dim3 blk(kFB, kFBY), grd((nx + kPatchX - 1) / kPatchX, (ny + kPatchY - 1) / kPatchY);
+  const dim3 blk(kFB, kFBY), grd(((nx + kPatchX - 1) / kPatchX) * ((ny + kPatchY - 1) / kPatchY));
   // union capacity from the input's mean segment count per column (24, 32,
   // 48 or 64; dense inputs take 48 up to 24 segments per column, which keeps
   // more warps per SM than 64, the rest going to the second tier)
